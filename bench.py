@@ -1,0 +1,346 @@
+"""Benchmark of the Limit-sticky9 force path on GB300: interactions/s of the integration step.
+
+Workload (the configuration the headline metric is quoted on): a Plummer sphere of
+N = 262,144 equal-mass stars in Henon units plus a BH of 0.01 x the stellar mass at the origin
+at rest (seeded, synthetic), eps = 0.01 * 4 / N^(1/3), dt = 1/1024, the reference's c = 1
+(inv_c2 = 1: every 1PN term on).  A step is one integration step of the reference's scheme
+(Limit-sticky9.c:844-893): three force() evaluations and the stage updates.  One interaction
+is one Newtonian (i, j) pair, n^2 per force() evaluation (n = N + 1), so a step is 3 n^2
+interactions.
+
+  value        mixed precision (FP32 pair terms, FP64 state/O(N) terms), state resident in HBM,
+               device time of K steps with CUDA events on the stream the kernels run on; the
+               L2 is overwritten (2x its size) before every timed step
+  e2e          the same metric through the reference-facing drop-in force() with host arrays,
+               as the reference's main loop calls it: per step 3 x (H2D x, v, m; D2H a) and the
+               stage updates on the host, wall clock
+  fp64         the FP64 path (parity with the reference) on the same workload
+  roofline     the pair-sweep kernel against the measured FP32 FMA peak of this GPU
+  cpu_baseline the oracle port of the reference (bit-identical to it) on a bounded sample of
+               rows of force() on the host cores, scaled to interactions/s
+
+--impl reference times the reference's CPU implementation of the path (the oracle port; the
+reference itself cannot be built on the GPU host) on all host cores, a bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NSTARS = 262144
+SEED = 2026
+BH_FRACTION = 0.01
+DT = 1.0 / 1024.0
+INV_C2 = 1.0
+METRIC = "interactions/s at N=2^18 (mixed FP32/FP64 integration step)"
+UNIT = "interactions/s"
+
+
+def workload_config(nstars=NSTARS):
+    import pn_gb300 as pn
+    return {"workload": f"plummer_bh_N{nstars}", "n_particles": nstars + 1,
+            "bh_mass_fraction": BH_FRACTION, "eps": pn.plummer_eps(nstars), "dt": DT,
+            "inv_c2": INV_C2, "step": "3 force() evaluations + stage updates (Limit-sticky9.c:844-893)",
+            "interaction": "one Newtonian (i,j) pair, n^2 per force()",
+            "l2": "2x L2 overwritten before each timed step"}
+
+
+def dist_init(n_gpus):
+    """torchrun env -> (rank, world, torch.distributed or None)."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+        return rank, world, dist
+    return 0, 1, None
+
+
+def max_over_ranks(val, dist):
+    if dist is None:
+        return val
+    import torch
+    t = torch.tensor([val], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while active."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, device=0):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [p.strip() for p in ln.split(",")]
+            if len(f) < 9 or not f[0].isdigit() or int(f[0]) != device:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(sysm, eps, seconds=12.0, threads=None):
+    """The oracle port on a bounded sample of force() rows (all three O(N^2) sweeps of each
+    row), timed on the host cores; returns interactions/s and the sample description."""
+    from oracle import pyoracle as po
+    po.build(ref=False)
+    threads = threads or os.cpu_count() or 1
+    n = sysm.x.shape[0]
+    rng = np.random.default_rng(1)
+    rows = np.sort(rng.choice(np.arange(1, n), size=threads * 2, replace=False))
+    t = po.time_force_rows(sysm.x, sysm.v, sysm.m, eps, rows, threads)  # calibration
+    per_row = t / rows.size * threads
+    k = max(threads, int(seconds * threads / max(per_row, 1e-6)))
+    k = min(k, n - 1)
+    rows = np.sort(rng.choice(np.arange(1, n), size=k, replace=False))
+    t = po.time_force_rows(sysm.x, sysm.v, sysm.m, eps, rows, threads)
+    rate = rows.size * n / t
+    return rate, {"rows": int(rows.size), "seconds": t, "threads": threads,
+                  "sample": f"{rows.size} random rows of force() at N={n - 1} (Newtonian row, "
+                            f"star cross row and BH cross row each), {threads} threads; "
+                            f"interactions = rows x n"}
+
+
+def run_reference(args, rank, world, dist):
+    """--impl reference: the reference's CPU path (oracle port) on all host cores."""
+    import pn_gb300 as pn
+    if rank != 0:
+        return 0
+    sysm = pn.config_plummer(NSTARS, SEED, BH_FRACTION)
+    eps = pn.plummer_eps(NSTARS)
+    threads = os.cpu_count() or 1
+    from oracle import pyoracle as po
+    po.build(ref=False)
+    n = sysm.x.shape[0]
+    rng = np.random.default_rng(7)
+    rows_per_step = threads * 4
+    times = []
+    for s in range(args.warmup + args.steps):
+        rows = np.sort(rng.choice(np.arange(1, n), size=rows_per_step, replace=False))
+        t = po.time_force_rows(sysm.x, sysm.v, sysm.m, eps, rows, threads)
+        if s >= args.warmup:
+            times.append(t)
+    total = sum(times)
+    value = args.steps * rows_per_step * n / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Plummer sphere + BH)", "config": workload_config(),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{rows_per_step} random rows of force() per step "
+                                       f"(all three O(N^2) sweeps per row), {threads} threads; "
+                                       "the reference source is not on the GPU host, so the "
+                                       "bit-identical C port of it runs"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def host_stage_step(pn, x, v, m, eps, dt):
+    """The reference main loop's step around the drop-in force() (Limit-sticky9.c:844-893)."""
+    a = pn.force(x, v, m, eps)
+    x1 = x + 0.5 * v * dt
+    v1 = v + 0.5 * a * dt
+    h = x1.copy()
+    hv = v1.copy()
+    a = pn.force(x1, v1, m, eps)
+    x1 = x + 0.5 * v1 * dt
+    v1 = v + 0.5 * a * dt
+    h += x1
+    hv += v1
+    a = pn.force(x1, v1, m, eps)
+    x3 = x + v1 * dt
+    v3 = v + a * dt
+    return (x + x3 + 2.0 * h) / 6.0, (v + v3 + 2.0 * hv) / 6.0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="pn", choices=["pn", "reference"])
+    ap.add_argument("--nstars", type=int, default=NSTARS)
+    ap.add_argument("--quick", action="store_true", help="skip the FP64, accuracy and CPU legs")
+    args = ap.parse_args()
+    rank, world, dist = dist_init(args.gpus)
+    if args.impl == "reference":
+        return run_reference(args, rank, world, dist)
+
+    import pn_gb300 as pn
+    from pn_gb300 import build as b
+    if not os.path.exists(pn.LIB_PATH):
+        b.build()
+    ns = args.nstars
+    n = ns + 1
+    sysm = pn.config_plummer(ns, SEED + rank, BH_FRACTION)
+    eps = pn.plummer_eps(ns)
+    out = {}
+
+    # ---------------- mixed precision, device resident (value)
+    ctx = pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=pn.PN_PREC_MIXED)
+    ctx.set_state(sysm.x, sysm.v, sysm.m)
+    ctx.bench_steps(args.warmup, flush_l2=True)
+    barrier(dist)
+    with ClockSampler() as clk:
+        t0 = time.perf_counter()
+        step_ms, pair_ms = ctx.bench_steps(args.steps, flush_l2=True)
+        wall = time.perf_counter() - t0
+    barrier(dist)
+    st = ctx.stats()
+    total_ms = max_over_ranks(float(step_ms.sum()), dist)
+    inter_step = 3.0 * n * n
+    value = world * args.steps * inter_step / (total_ms * 1e-3)
+    ms_per_step = total_ms / args.steps
+    pair_launch_ms = float(pair_ms.mean()) / 3.0
+    ctx.close()
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded Plummer sphere + BH)",
+            "config": dict(workload_config(ns), parallelism=f"replicas{world}" if world > 1 else "1 GPU",
+                           pair_kernel={"tile_j": st.tile_j, "i_per_thread": st.i_per_thread,
+                                        "j_split": st.j_split, "grid_split": st.grid_split,
+                                        "threads": st.threads}),
+            "gpu_launches": 9 * args.steps,
+            "clocks": clk.summary(int(os.environ.get("LOCAL_RANK", "0")))}
+
+    # roofline of the pair sweep against the measured FP32 FMA peak
+    if rank == 0:
+        flops_pair = pn.flops_per_pair(1, pn.PN_PREC_MIXED)
+        peak32 = pn.probe_fma_peak(pn.PN_PREC_MIXED)
+        pairs = float(ns) * float(ns)
+        achieved = pairs * flops_pair / (pair_launch_ms * 1e-3) / 1e12
+        line["roofline"] = {"bound": "fp32", "kernel": "k_pair<float, MODE_FORCE>",
+                            "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
+                            "frac": achieved / peak32, "traffic": None,
+                            "flops_per_pair": flops_pair,
+                            "pair_launch_ms": pair_launch_ms,
+                            "peak_source": "measured FP32 FMA throughput of this GPU (pn_probe_fma_peak)",
+                            "pair_interactions_per_s": pairs / (pair_launch_ms * 1e-3)}
+        prof = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(prof):
+            try:
+                line["roofline"]["traffic"] = json.load(open(prof)).get("k_pair_force_f32_bytes_per_launch")
+            except (OSError, ValueError):
+                pass
+
+    # ---------------- e2e through the drop-in force() with host arrays
+    pn.configure(pn.PN_PREC_MIXED, INV_C2)
+    x, v = sysm.x.copy(), sysm.v.copy()
+    x, v = host_stage_step(pn, x, v, sysm.m, eps, DT)  # warm-up
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        x, v = host_stage_step(pn, x, v, sysm.m, eps, DT)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+    pn.configure(pn.PN_PREC_FP64, INV_C2)
+    pn.lib().pn_dropin_release()
+    line["e2e"] = {"value": world * e2e_steps * inter_step / e2e_s, "unit": UNIT,
+                   "h2d_bytes_per_step": 3 * (2 * 24 + 8) * n, "d2h_bytes_per_step": 3 * 24 * n,
+                   "path": "drop-in force() x3 per step with host arrays + host stage updates"}
+    line["gpu_launches"] += 9 * e2e_steps
+
+    if rank == 0 and not args.quick:
+        # ---------------- FP64 path on the same workload (one step) and mixed accuracy
+        c64 = pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=pn.PN_PREC_FP64)
+        c64.set_state(sysm.x, sysm.v, sysm.m)
+        a64 = c64.force()
+        sm64, pm64 = c64.bench_steps(1, flush_l2=True)
+        c64.close()
+        line["fp64"] = {"value": inter_step / (sm64[0] * 1e-3), "unit": UNIT,
+                        "ms_per_step": float(sm64[0]),
+                        "peak_fp64_tflops": pn.probe_fma_peak(pn.PN_PREC_FP64),
+                        "pair_tflops": float(ns) * ns * pn.flops_per_pair(1, 0) / (pm64[0] / 3 * 1e-3) / 1e12}
+        line["mixed_over_fp64"] = value / world / line["fp64"]["value"]
+        acc = {}
+        for ic2 in (INV_C2, 1e-6):
+            cm = pn.Context(n, eps=eps, inv_c2=ic2, precision=pn.PN_PREC_MIXED)
+            cm.set_state(sysm.x, sysm.v, sysm.m)
+            a32 = cm.force()
+            cm.close()
+            if ic2 != INV_C2:
+                cd = pn.Context(n, eps=eps, inv_c2=ic2, precision=pn.PN_PREC_FP64)
+                cd.set_state(sysm.x, sysm.v, sysm.m)
+                ref = cd.force()
+                cd.close()
+            else:
+                ref = a64
+            d = np.linalg.norm(a32 - ref, axis=1)
+            r = d / np.linalg.norm(ref, axis=1)
+            acc[f"inv_c2={ic2:g}"] = {
+                "rms_rel": float(np.sqrt((r ** 2).mean())), "max_rel": float(r.max()),
+                "rms_abs_over_rms_a": float(np.sqrt((d ** 2).mean() / (np.linalg.norm(ref, axis=1) ** 2).mean()))}
+        line["accuracy_vs_fp64"] = acc
+        # ---------------- CPU baseline (oracle port), bounded sample
+        rate, info = cpu_baseline(sysm, eps)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": info["threads"], "kind": "port",
+                                "sample": info["sample"], "seconds": info["seconds"]}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,177 @@
+/*
+ * pn.h -- C ABI of libpn: the Limit-sticky9 direct-summation force path on one GB300 (sm_103a).
+ *
+ * Three layers, all plain C types (no CUDA or torch types in any signature):
+ *
+ *  1. Drop-in entry points with the reference's own names and signatures, so the reference's
+ *     main loop (Limit-sticky9.c:740-920) links against this library unchanged:
+ *       force            replaces Limit-sticky9.c:21-424
+ *       energy           replaces Limit-sticky9.c:427-564  (prints the same three lines)
+ *       initial_energy   replaces Limit-sticky9.c:566-714  (prints the same two lines)
+ *       push_velocity / push_position   replace Limit-sticky9.c:716-738 (host loops, unused
+ *                                        by the reference main; kept for link compatibility)
+ *     Arrays are the caller's host AoS arrays double[n][3] with index 0 = the black hole (BH),
+ *     exactly as in the reference.  Each call copies x, v, m to the GPU and the result back,
+ *     as the Goose-generated GPU variant did.  Errors: these keep the reference's void
+ *     signatures; pn_last_error() reports the last status, and a CUDA failure aborts with a
+ *     message (the Goose variant called exit(1), Limit-sticky9_nvidia.cu:89-114).
+ *
+ *  2. A device-resident context (pn_ctx) that keeps the state on the GPU between force
+ *     evaluations and runs whole integration steps (the reference's 3-evaluation
+ *     Runge-Kutta step, Limit-sticky9.c:841-893) as one CUDA graph per step.
+ *
+ *  3. Host utilities: initial-condition generators and the reference's text formats
+ *     (input Limit-sticky9.c:796-809, snapshots :820-826 / :899-905).
+ *
+ * Units are G = 1; the 1PN terms are weighted by inv_c2 (1.0 reproduces the reference,
+ * which has c = 1 implicitly; 0.0 gives the Newtonian force alone).  All functions returning
+ * int return PN_OK (0) or a negative pn_status.
+ */
+#ifndef PN_H
+#define PN_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PN_NMAX 270000 /* Limit-sticky9.c:13: the drop-in entry points accept n <= PN_NMAX */
+
+typedef enum {
+    PN_OK = 0,
+    PN_ERR_INVALID = -1,     /* bad argument (n out of range, NULL pointer, eps <= 0, ...) */
+    PN_ERR_CUDA = -2,        /* a CUDA runtime call failed */
+    PN_ERR_NOMEM = -3,       /* device or host allocation failed */
+    PN_ERR_NONFINITE = -4,   /* a force or energy came out NaN/Inf */
+    PN_ERR_IO = -5,          /* file open/parse error */
+    PN_ERR_TIMEOUT = -6,     /* a bounded in-kernel wait gave up (the kernel returned early) */
+    PN_ERR_UNSUPPORTED = -7, /* no GPU, or a configuration this build does not support */
+    PN_ERR_STATE = -8        /* call out of order (e.g. no state set) */
+} pn_status;
+
+typedef enum {
+    PN_PREC_FP64 = 0,  /* every pair term in FP64: parity with the reference */
+    PN_PREC_MIXED = 1  /* FP32 pair terms (per-tile FP64 origin, compensated sums), FP64 rest */
+} pn_precision;
+
+typedef struct {
+    double eps;        /* Plummer softening (Limit-sticky9.c:770) */
+    double dt;         /* time step (Limit-sticky9.c:771) */
+    double inv_c2;     /* weight of the 1PN terms; 1.0 = reference */
+    int precision;     /* pn_precision */
+    int tile_j;        /* j-particles per shared-memory tile; 0 = tuned */
+    int i_per_thread;  /* i-particles held per thread; 0 = tuned */
+    int j_split;       /* lanes sharing one i-set (warp-shuffle reduction); 0 = tuned */
+    int grid_split;    /* CTAs sharing one i-block (partial sums reduced in FP64); 0 = tuned */
+} pn_params;
+
+/* Energies as the reference prints them (Limit-sticky9.c:561-562, :702-703). */
+typedef struct {
+    double pot_n;  /* Newtonian potential energy */
+    double kin_n;  /* Newtonian kinetic energy */
+    double pot_pn; /* O(N) 1PN BH-star energy */
+    double total;  /* kin_n + pot_n + pot_pn + sum of the pairwise 1PN energy */
+} pn_energy_t;
+
+/* Kernel timing/accounting of the last device operation (for benchmarks). */
+typedef struct {
+    double pair_ms;          /* time of the last O(N^2) pair kernel launch (CUDA events) */
+    double total_ms;         /* whole force evaluation */
+    double interactions;     /* star-star pairs evaluated by that launch */
+    int tile_j, i_per_thread, j_split, grid_split, threads; /* launch shape used */
+} pn_stats;
+
+/* ------------------------------------------------------------------ 1. drop-in entry points */
+void force(double (*x)[3], double (*v)[3], double *m, double eps, double (*a)[3], double *pot,
+           int n);
+void energy(double t, double x[][3], double v[][3], double m[], int n, double init_ene,
+            double eps);
+void initial_energy(double x[][3], double v[][3], double m[], int n, double *init_ene,
+                    double eps);
+void push_velocity(double v[][3], double a[][3], double dt, int n);
+void push_position(double x[][3], double v[][3], double dt, int n);
+
+/* Status of the last drop-in call on this thread (PN_OK after a successful one). */
+int pn_last_error(void);
+/* Human-readable detail of the last error on this thread ("" when none). */
+const char *pn_last_error_message(void);
+const char *pn_strerror(int status);
+/* Precision of the drop-in entry points (default PN_PREC_FP64; the environment variable
+ * PN_PRECISION=mixed selects PN_PREC_MIXED at first use).  Also sets inv_c2 for them. */
+int pn_dropin_configure(int precision, double inv_c2);
+/* Releases the drop-in entry points' implicit context (optional; also done at exit). */
+void pn_dropin_release(void);
+
+/* ------------------------------------------------------------------ 2. device-resident API */
+typedef struct pn_ctx pn_ctx;
+
+void pn_params_default(pn_params *p);
+/* Creates a context for up to nmax particles (BH included) on the current CUDA device. */
+int pn_create(pn_ctx **ctx, int nmax, const pn_params *p);
+int pn_destroy(pn_ctx *ctx);
+/* Host AoS [n][3] state in / out (index 0 = BH). */
+int pn_set_state(pn_ctx *ctx, int n, const double *x, const double *v, const double *m);
+int pn_get_state(pn_ctx *ctx, double *x, double *v);
+/* Acceleration at the current state into host AoS a[n][3] (one force() evaluation). */
+int pn_force(pn_ctx *ctx, double *a);
+/* nsteps integration steps of the reference's scheme (Limit-sticky9.c:844-893) on the
+ * device-resident state; time advances by dt per step.  Asynchronous on the context's
+ * stream: pn_sync() waits and returns the status of in-kernel checks. */
+int pn_steps(pn_ctx *ctx, int nsteps);
+int pn_sync(pn_ctx *ctx);
+/* Energies of the current state (Limit-sticky9.c:445-556 arithmetic). */
+int pn_energy(pn_ctx *ctx, pn_energy_t *e);
+double pn_time(pn_ctx *ctx);
+int pn_get_stats(pn_ctx *ctx, pn_stats *s);
+/* Changes the run parameters of an existing context (e.g. precision). */
+int pn_set_params(pn_ctx *ctx, const pn_params *p);
+
+/* Device-pointer entry point: one force evaluation on caller-owned device AoS arrays
+ * (d_x, d_v: double[n][3]; d_m: double[n]; d_a: double[n][3] out) on the given stream
+ * (a cudaStream_t passed as void*; NULL = the context's stream). */
+int pn_force_device(pn_ctx *ctx, int n, const double *d_x, const double *d_v,
+                    const double *d_m, double *d_a, void *stream);
+
+/* Benchmark support.  Runs nsteps captured integration steps one at a time on the context's
+ * stream; before each, optionally overwrites a buffer twice the size of L2 (flush_l2 != 0).
+ * step_ms[k]: CUDA-event time of step k; pair_ms[k]: summed time of its three pair-sweep
+ * launches (events captured in the step graph around each launch). */
+int pn_bench_steps(pn_ctx *ctx, int nsteps, int flush_l2, double *step_ms, double *pair_ms);
+/* Flops of one pair interaction of a sweep (mode 0 Newtonian, 1 force with 1PN, 2 energy) in
+ * the given precision; an FMA counts 2, the MUFU rsqrt 1, any other add or multiply 1. */
+double pn_flops_per_pair(int mode, int precision);
+/* Measured FMA throughput of this GPU (TFLOP/s, FMA = 2 flops) in FP32 (PN_PREC_MIXED) or
+ * FP64 (PN_PREC_FP64): the roofline denominator of the pair sweeps. */
+int pn_probe_fma_peak(int precision, double *tflops);
+
+/* Self-test of the in-kernel bounded waits: launches a kernel whose mbarrier wait can only end
+ * by its time limit (about `seconds`, at most 5); returns PN_ERR_TIMEOUT when the limit
+ * worked and the kernel returned on its own.  Faults nothing; the context stays usable. */
+int pn_selftest_wait_timeout(pn_ctx *ctx, double seconds);
+
+/* ------------------------------------------------------------------ 3. host utilities */
+/* nstars stars uniform in a ball of the given radius (r = R u^(1/3), isotropic), v = 0.
+ * x, v: [nstars][3].  Deterministic for a given seed on every platform. */
+int pn_ic_uniform_sphere(int nstars, double radius, uint64_t seed, double *x, double *v);
+/* nstars stars from a Plummer sphere in Henon units (M = 1, E = -1/4) by the
+ * Aarseth-Henon-Wielen (1974) method, shifted to the centre-of-mass frame. */
+int pn_ic_plummer(int nstars, uint64_t seed, double *x, double *v);
+/* The reference's input format (Limit-sticky9.c:796-809): nstars lines "x y z" then nstars
+ * lines "vx vy vz"; values are parsed as float and widened to double, as the reference does.
+ * The BH is not in the file. */
+int pn_read_init(const char *path, int nstars, double *x, double *v);
+int pn_write_init(const char *path, int nstars, const double *x, const double *v);
+/* Snapshot block as the reference writes it (Limit-sticky9.c:820-826): n lines of x then n
+ * lines of v with "%lf %lf %lf \n".  append != 0 appends to the file. */
+int pn_write_snapshot(const char *path, int n, const double *x, const double *v, int append);
+
+/* Number of CUDA devices visible (0 on a machine without a GPU); never aborts. */
+int pn_device_count(void);
+const char *pn_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PN_H */

@@ -1,0 +1,40 @@
+// pn_internal.h -- host-side declarations shared by libpn's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "pn_pair.cuh"
+
+namespace pn {
+
+struct PairCfg {
+    int ipt = 2;     // i-particles per thread
+    int js = 1;      // lanes sharing one i-set
+    int tj = 128;    // stars per j-tile
+    int gsplit = 1;  // j-range splits across CTAs
+};
+
+// Launches k_pair for the given precision/mode/shape (returns cudaErrorInvalidValue for an
+// unsupported (ipt, js) combination).  Implemented in pn_pair_f32.cu / pn_pair_f64.cu.
+cudaError_t launch_pair_f32(int mode, const PairCfg &c, const PairArgs &a, cudaStream_t s);
+cudaError_t launch_pair_f64(int mode, const PairCfg &c, const PairArgs &a, cudaStream_t s);
+bool pair_shape_supported(int ipt, int js);
+
+inline int pair_ng(bool f32, int mode) {
+    if (f32) return mode == MODE_NEWTON ? ModeInfo<MODE_NEWTON>::NG32
+                  : mode == MODE_FORCE  ? ModeInfo<MODE_FORCE>::NG32
+                                        : ModeInfo<MODE_ENERGY>::NG32;
+    return mode == MODE_NEWTON ? ModeInfo<MODE_NEWTON>::NG64
+         : mode == MODE_FORCE  ? ModeInfo<MODE_FORCE>::NG64
+                               : ModeInfo<MODE_ENERGY>::NG64;
+}
+
+inline int pair_nacc(int mode) {
+    return mode == MODE_NEWTON ? ModeInfo<MODE_NEWTON>::NACC
+         : mode == MODE_FORCE  ? ModeInfo<MODE_FORCE>::NACC
+                               : ModeInfo<MODE_ENERGY>::NACC;
+}
+
+inline int pair_block_i(const PairCfg &c) { return PAIR_NT * c.ipt / c.js; }
+
+}  // namespace pn

@@ -1,0 +1,48 @@
+// pn_pair_f32.cu -- instantiations and launcher of the float pair-sweep kernel (see pn_pair.cuh).
+#include "pn_internal.h"
+
+namespace pn {
+
+template <int MODE, int IPT, int JS>
+static cudaError_t launch_one(const PairCfg &c, const PairArgs &a, cudaStream_t s) {
+    constexpr bool F32 = sizeof(float) == 4;
+    const int ng = F32 ? ModeInfo<MODE>::NG32 : ModeInfo<MODE>::NG64;
+    const size_t smem = pair_smem_bytes(ng, c.tj, sizeof(float4));
+    auto fn = k_pair<float, MODE, IPT, JS>;
+    static size_t configured = 0;  // largest dynamic smem size enabled so far
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    const int bi = PAIR_NT * IPT / JS;
+    dim3 grid((unsigned)((a.nstar + bi - 1) / bi), (unsigned)c.gsplit);
+    fn<<<grid, PAIR_NT, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <int MODE>
+static cudaError_t launch_mode(const PairCfg &c, const PairArgs &a, cudaStream_t s) {
+    if (c.js == 1) {
+        if (c.ipt == 1) return launch_one<MODE, 1, 1>(c, a, s);
+        if (c.ipt == 2) return launch_one<MODE, 2, 1>(c, a, s);
+        if (c.ipt == 4) return launch_one<MODE, 4, 1>(c, a, s);
+    } else if (c.ipt == 1) {
+        if (c.js == 2) return launch_one<MODE, 1, 2>(c, a, s);
+        if (c.js == 4) return launch_one<MODE, 1, 4>(c, a, s);
+        if (c.js == 8) return launch_one<MODE, 1, 8>(c, a, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_pair_f32(int mode, const PairCfg &c, const PairArgs &a, cudaStream_t s) {
+    if (a.nstar <= 0) return cudaSuccess;
+    switch (mode) {
+        case MODE_NEWTON: return launch_mode<MODE_NEWTON>(c, a, s);
+        case MODE_FORCE: return launch_mode<MODE_FORCE>(c, a, s);
+        case MODE_ENERGY: return launch_mode<MODE_ENERGY>(c, a, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace pn
