@@ -2,8 +2,8 @@
 
 Workload (the configuration the headline metric is quoted on): a Plummer sphere of
 N = 262,144 equal-mass stars in Henon units plus a BH of 0.01 x the stellar mass at the origin
-at rest (seeded, synthetic), eps = 0.01 * 4 / N^(1/3), dt = 1/1024, the reference's c = 1
-(inv_c2 = 1: every 1PN term on).  A step is one integration step of the reference's scheme
+at rest (seeded, synthetic), eps = 0.01 * 4 / N^(1/3), dt = 1/1024, c = 1000 (inv_c2 = 1e-6; every
+1PN term is evaluated, as small corrections).  A step is one integration step of the reference's scheme
 (Limit-sticky9.c:844-893): three force() evaluations and the stage updates.  One interaction
 is one Newtonian (i, j) pair, n^2 per force() evaluation (n = N + 1), so a step is 3 n^2
 interactions.
@@ -42,7 +42,10 @@ NSTARS = 262144
 SEED = 2026
 BH_FRACTION = 0.01
 DT = 1.0 / 1024.0
-INV_C2 = 1.0
+# c = 1000 in these units: the 1PN terms are corrections to the Newtonian force.  (With the
+# reference's implicit c = 1 a Hénon-unit Plummer sphere has v/c ~ 1 and its 1PN "corrections"
+# are O(1): the energy runs away within a few steps.)  The kernels do the same work for any c.
+INV_C2 = 1e-6
 METRIC = "interactions/s at N=2^18 (mixed FP32/FP64 integration step)"
 UNIT = "interactions/s"
 
@@ -70,12 +73,19 @@ def dist_init(n_gpus):
 
 
 def max_over_ranks(val, dist):
+    """The slowest rank's time (replicas run independently; the job ends with the last)."""
     if dist is None:
         return val
     import torch
-    t = torch.tensor([val], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([val], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(world, steps, units_per_step, slowest_seconds):
+    """Whole-job throughput of `world` independent replicas: all units over the slowest time."""
+    return world * steps * units_per_step / slowest_seconds
 
 
 def barrier(dist):
@@ -193,6 +203,21 @@ def run_reference(args, rank, world, dist):
     return 0
 
 
+def profile_case(nstars):
+    """One mixed-precision force evaluation of the bench workload at nstars (ncu target)."""
+    import pn_gb300 as pn
+    sysm = pn.config_plummer(nstars, SEED, BH_FRACTION)
+    with pn.Context(nstars + 1, eps=pn.plummer_eps(nstars), inv_c2=INV_C2,
+                    precision=pn.PN_PREC_MIXED) as c:
+        c.set_state(sysm.x, sysm.v, sysm.m)
+        c.force()
+        st = c.stats()
+        print(json.dumps({"profile_case": nstars, "pair_ms": st.pair_ms, "tile_j": st.tile_j,
+                          "i_per_thread": st.i_per_thread, "j_split": st.j_split,
+                          "grid_split": st.grid_split}))
+    return 0
+
+
 def host_stage_step(pn, x, v, m, eps, dt):
     """The reference main loop's step around the drop-in force() (Limit-sticky9.c:844-893)."""
     a = pn.force(x, v, m, eps)
@@ -219,7 +244,11 @@ def main():
     ap.add_argument("--impl", default="pn", choices=["pn", "reference"])
     ap.add_argument("--nstars", type=int, default=NSTARS)
     ap.add_argument("--quick", action="store_true", help="skip the FP64, accuracy and CPU legs")
+    ap.add_argument("--profile-case", type=int, default=0, metavar="N",
+                    help="set up N stars, tune, run one mixed force evaluation and exit (for ncu)")
     args = ap.parse_args()
+    if args.profile_case:
+        return profile_case(args.profile_case)
     rank, world, dist = dist_init(args.gpus)
     if args.impl == "reference":
         return run_reference(args, rank, world, dist)
@@ -237,6 +266,7 @@ def main():
     # ---------------- mixed precision, device resident (value)
     ctx = pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=pn.PN_PREC_MIXED)
     ctx.set_state(sysm.x, sysm.v, sysm.m)
+    ctx.autotune(1)  # setup: launch shape of the pair sweep for this size (not timed)
     ctx.bench_steps(args.warmup, flush_l2=True)
     barrier(dist)
     with ClockSampler() as clk:
@@ -247,7 +277,7 @@ def main():
     st = ctx.stats()
     total_ms = max_over_ranks(float(step_ms.sum()), dist)
     inter_step = 3.0 * n * n
-    value = world * args.steps * inter_step / (total_ms * 1e-3)
+    value = replica_throughput(world, args.steps, inter_step, total_ms * 1e-3)
     ms_per_step = total_ms / args.steps
     pair_launch_ms = float(pair_ms.mean()) / 3.0
     ctx.close()
@@ -295,7 +325,7 @@ def main():
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
     pn.configure(pn.PN_PREC_FP64, INV_C2)
     pn.lib().pn_dropin_release()
-    line["e2e"] = {"value": world * e2e_steps * inter_step / e2e_s, "unit": UNIT,
+    line["e2e"] = {"value": replica_throughput(world, e2e_steps, inter_step, e2e_s), "unit": UNIT,
                    "h2d_bytes_per_step": 3 * (2 * 24 + 8) * n, "d2h_bytes_per_step": 3 * 24 * n,
                    "path": "drop-in force() x3 per step with host arrays + host stage updates"}
     line["gpu_launches"] += 9 * e2e_steps
@@ -313,7 +343,7 @@ def main():
                         "pair_tflops": float(ns) * ns * pn.flops_per_pair(1, 0) / (pm64[0] / 3 * 1e-3) / 1e12}
         line["mixed_over_fp64"] = value / world / line["fp64"]["value"]
         acc = {}
-        for ic2 in (INV_C2, 1e-6):
+        for ic2 in (INV_C2, 1.0):
             cm = pn.Context(n, eps=eps, inv_c2=ic2, precision=pn.PN_PREC_MIXED)
             cm.set_state(sysm.x, sysm.v, sysm.m)
             a32 = cm.force()

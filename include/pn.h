@@ -127,11 +127,26 @@ int pn_get_stats(pn_ctx *ctx, pn_stats *s);
 /* Changes the run parameters of an existing context (e.g. precision). */
 int pn_set_params(pn_ctx *ctx, const pn_params *p);
 
+/* Binary checkpoint of a context (state, masses, time, parameters) plus the driver's snapshot
+ * clock and initial energy; pn_load_checkpoint restores all of it into an existing context
+ * (n must fit its capacity).  Format: "PNCK0001", int32 n, doubles time, eouttime, init_ene,
+ * the pn_params struct, then x, v (AoS [n][3]) and m [n], little-endian. */
+int pn_save_checkpoint(pn_ctx *ctx, const char *path, double eouttime, double init_ene);
+int pn_load_checkpoint(pn_ctx *ctx, const char *path, double *eouttime, double *init_ene);
+
 /* Device-pointer entry point: one force evaluation on caller-owned device AoS arrays
  * (d_x, d_v: double[n][3]; d_m: double[n]; d_a: double[n][3] out) on the given stream
  * (a cudaStream_t passed as void*; NULL = the context's stream). */
 int pn_force_device(pn_ctx *ctx, int n, const double *d_x, const double *d_v,
                     const double *d_m, double *d_a, void *stream);
+
+/* Launch-shape autotuner.  Times candidate shapes of the pair sweep on the context's current
+ * state (sweeps: bit 0 = the force sweep, bit 1 = the energy sweep) and keeps the fastest per
+ * (precision, sweep, size class floor(log2 N)) for every context of this process; with the
+ * environment variable PN_TUNE_CACHE=<file> the table is also kept in that file.  Shapes set
+ * explicitly in pn_params take precedence.  best_ms (optional, [2]) gets the winning times. */
+int pn_autotune(pn_ctx *ctx, int sweeps, double *best_ms);
+void pn_autotune_clear(void);
 
 /* Benchmark support.  Runs nsteps captured integration steps one at a time on the context's
  * stream; before each, optionally overwrites a buffer twice the size of L2 (flush_l2 != 0).
@@ -149,6 +164,52 @@ int pn_probe_fma_peak(int precision, double *tflops);
  * by its time limit (about `seconds`, at most 5); returns PN_ERR_TIMEOUT when the limit
  * worked and the kernel returned on its own.  Faults nothing; the context stays usable. */
 int pn_selftest_wait_timeout(pn_ctx *ctx, double seconds);
+
+/* ------------------------------------------------------------------ 2a. discrete adjoint */
+/* Vector-Jacobian product of one force evaluation at the current state: for abar (host AoS
+ * [n][3], the adjoint of the accelerations) returns xbar = (da/dx)^T abar, vbar = (da/dv)^T
+ * abar (host AoS [n][3]) and m0bar = abar . da/dm0 (the BH mass).  Same precision as the
+ * context (FP64, or FP32 pair terms in mixed mode). */
+int pn_force_vjp(pn_ctx *ctx, const double *abar, double *xbar, double *vbar, double *m0bar);
+/* Gradients through nsteps integration steps (Limit-sticky9.c:844-893).  pn_adj_forward runs
+ * the steps from the current state, keeping the state every checkpoint_every steps on the GPU;
+ * the context then holds the final state (read it with pn_get_state to form the loss).
+ * pn_adj_backward takes dL/dx(T), dL/dv(T) (host AoS) and returns dL/dx(0), dL/dv(0) and
+ * dL/dm0: each segment between checkpoints is recomputed from its checkpoint (stage states and
+ * pair sums kept for the segment) and reversed stage by stage, one force VJP per stage.  The
+ * context's state is the final state again afterwards. */
+int pn_adj_forward(pn_ctx *ctx, int nsteps, int checkpoint_every);
+int pn_adj_backward(pn_ctx *ctx, const double *xbar_T, const double *vbar_T, double *xbar_0,
+                    double *vbar_0, double *m0bar);
+
+/* ------------------------------------------------------------------ 2b. ensembles */
+/* Many independent systems (each a BH + stars, the reference's model) advanced together: one
+ * launch per kernel for the whole ensemble, the O(N^2) sweep of every cluster in ONE persistent
+ * launch over a shared work queue, each integration step captured in one CUDA graph.  All
+ * clusters share dt, inv_c2 and the precision; eps is per cluster.  Arrays are the clusters'
+ * AoS arrays concatenated: cluster c occupies rows [sum_{c'<c} n[c'], ... + n[c]), its BH
+ * first. */
+typedef struct pn_ens pn_ens;
+int pn_ens_create(pn_ens **ens, int nclusters, const int *n, const double *eps, const pn_params *p);
+int pn_ens_destroy(pn_ens *ens);
+int pn_ens_set_state(pn_ens *ens, const double *x, const double *v, const double *m);
+int pn_ens_get_state(pn_ens *ens, double *x, double *v);
+int pn_ens_force(pn_ens *ens, double *a);
+int pn_ens_steps(pn_ens *ens, int nsteps);
+int pn_ens_sync(pn_ens *ens);
+/* Energies per cluster: out[4c + 0..3] = pot_n, kin_n, pot_pn, total. */
+int pn_ens_energy(pn_ens *ens, double *out);
+double pn_ens_time(pn_ens *ens);
+int pn_ens_last_error(void);
+/* Times nsteps captured steps one by one (CUDA events on the ensemble's stream). */
+int pn_ens_bench_steps(pn_ens *ens, int nsteps, double *step_ms);
+/* Autotuner: per size class (floor(log2 N)) the j-tile size and the j-range of one work item
+ * (in tiles), then the launch's i per thread and lanes per i-set, timed on the live state. */
+int pn_ens_autotune(pn_ens *ens);
+/* Explicit shapes: ipt/js (0 = keep) and, for size_class >= 0, that class's tile size and
+ * work-item length. */
+int pn_ens_set_shape(pn_ens *ens, int ipt, int js, int size_class, int tile_j, int tiles_per_item);
+int pn_ens_get_shape(pn_ens *ens, int size_class, int *ipt, int *js, int *tile_j, int *tiles_per_item);
 
 /* ------------------------------------------------------------------ 3. host utilities */
 /* nstars stars uniform in a ball of the given radius (r = R u^(1/3), isotropic), v = 0.

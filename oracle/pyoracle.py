@@ -23,6 +23,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libpn_oracle.so")
+ORACLE_LD_SO = os.path.join(HERE, "_build", "libpn_oracle_ld.so")
 REF_SO = os.path.join(HERE, "_ref", "libls9ref.so")
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -48,6 +49,7 @@ def reference_source_present() -> bool:
 
 _lib = None
 _ref = None
+_ld = None
 
 
 def lib():
@@ -70,6 +72,36 @@ def lib():
         L.orc_force_rows.restype = ctypes.c_int
         _lib = L
     return _lib
+
+
+def lib_ld():
+    """The long-double build of the restatement (exact reference for rounding checks)."""
+    global _ld
+    if _ld is None:
+        if not os.path.exists(ORACLE_LD_SO):
+            build(ref=False)
+        L = ctypes.CDLL(ORACLE_LD_SO)
+        L.orcld_force_d.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, _dp]
+        L.orcld_force_d.restype = None
+        L.orcld_energy_d.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, _dp]
+        L.orcld_energy_d.restype = ctypes.c_double
+        _ld = L
+    return _ld
+
+
+def force_exact(x, v, m, eps):
+    """force() evaluated in long double, rounded to double at the end."""
+    x, v, m = _state(x, v, m)
+    a = np.zeros_like(x)
+    lib_ld().orcld_force_d(x.shape[0], _ptr(x), _ptr(v), _ptr(m), float(eps), _ptr(a))
+    return a
+
+
+def energy_exact(x, v, m, eps):
+    x, v, m = _state(x, v, m)
+    out = np.zeros(4)
+    lib_ld().orcld_energy_d(x.shape[0], _ptr(x), _ptr(v), _ptr(m), float(eps), _ptr(out))
+    return out
 
 
 def ref_available() -> bool:

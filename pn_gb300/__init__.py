@@ -93,11 +93,32 @@ SIGNATURES = [
     ("pn_force_device", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p]),
+    ("pn_force_vjp", ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
+    ("pn_adj_forward", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    ("pn_adj_backward", ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp]),
+    ("pn_ens_create", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_int), _dp, ctypes.POINTER(Params)]),
+    ("pn_ens_destroy", ctypes.c_int, [ctypes.c_void_p]),
+    ("pn_ens_set_state", ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp]),
+    ("pn_ens_get_state", ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
+    ("pn_ens_force", ctypes.c_int, [ctypes.c_void_p, _dp]),
+    ("pn_ens_steps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    ("pn_ens_sync", ctypes.c_int, [ctypes.c_void_p]),
+    ("pn_ens_energy", ctypes.c_int, [ctypes.c_void_p, _dp]),
+    ("pn_ens_time", ctypes.c_double, [ctypes.c_void_p]),
+    ("pn_ens_last_error", ctypes.c_int, []),
+    ("pn_ens_bench_steps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
+    ("pn_ens_autotune", ctypes.c_int, [ctypes.c_void_p]),
+    ("pn_ens_set_shape", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_int]),
+    ("pn_ens_get_shape", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 4),
     ("pn_ic_uniform_sphere", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_uint64, _dp, _dp]),
     ("pn_ic_plummer", ctypes.c_int, [ctypes.c_int, ctypes.c_uint64, _dp, _dp]),
     ("pn_read_init", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _dp, _dp]),
     ("pn_write_init", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _dp, _dp]),
     ("pn_write_snapshot", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _dp, _dp, ctypes.c_int]),
+    ("pn_autotune", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
+    ("pn_autotune_clear", None, []),
     ("pn_bench_steps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     ("pn_flops_per_pair", ctypes.c_double, [ctypes.c_int, ctypes.c_int]),
     ("pn_probe_fma_peak", ctypes.c_int, [ctypes.c_int, _dp]),
@@ -268,6 +289,35 @@ class Context:
         _check(lib().pn_get_stats(self._h, ctypes.byref(s)), "pn_get_stats")
         return s
 
+    def autotune(self, sweeps: int = 1):
+        """Tunes the pair-sweep launch shape on the current state; returns the best times (ms)."""
+        t = np.zeros(2)
+        _check(lib().pn_autotune(self._h, int(sweeps), _p(t)), "pn_autotune")
+        return t
+
+    def force_vjp(self, abar):
+        """(xbar, vbar, m0bar) = VJP of the force at the current state with adjoint abar."""
+        ab = _aos(abar, self.n)
+        xb = np.zeros((self.n, 3))
+        vb = np.zeros((self.n, 3))
+        m0 = np.zeros(1)
+        _check(lib().pn_force_vjp(self._h, _p(ab), _p(xb), _p(vb), _p(m0)), "pn_force_vjp")
+        return xb, vb, float(m0[0])
+
+    def adjoint_forward(self, nsteps: int, checkpoint_every: int):
+        _check(lib().pn_adj_forward(self._h, int(nsteps), int(checkpoint_every)), "pn_adj_forward")
+
+    def adjoint_backward(self, xbar_T, vbar_T):
+        """(dL/dx0, dL/dv0, dL/dm0) from dL/dx(T), dL/dv(T) after adjoint_forward."""
+        xb = _aos(xbar_T, self.n)
+        vb = _aos(vbar_T, self.n)
+        x0 = np.zeros((self.n, 3))
+        v0 = np.zeros((self.n, 3))
+        m0 = np.zeros(1)
+        _check(lib().pn_adj_backward(self._h, _p(xb), _p(vb), _p(x0), _p(v0), _p(m0)),
+               "pn_adj_backward")
+        return x0, v0, float(m0[0])
+
     def bench_steps(self, k: int, flush_l2: bool = True):
         """Times k integration steps (CUDA events on the context's stream).  Returns
         (step_ms[k], pair_ms[k])."""
@@ -280,6 +330,91 @@ class Context:
     def force_device(self, n, d_x, d_v, d_m, d_a, stream=None):
         """One evaluation on caller-owned device AoS buffers (raw device pointers)."""
         _check(lib().pn_force_device(self._h, int(n), d_x, d_v, d_m, d_a, stream), "pn_force_device")
+
+
+class Ensemble:
+    """Independent clusters advanced together (``pn_ens``).  ``systems`` is a list of
+    :class:`System`; ``eps`` one softening per cluster."""
+
+    def __init__(self, systems, eps, **params):
+        _require_gpu()
+        self.sizes = [s.x.shape[0] for s in systems]
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(int)
+        self.params = default_params(**params)
+        n = (ctypes.c_int * len(systems))(*self.sizes)
+        e = np.ascontiguousarray(eps, dtype=np.float64)
+        h = ctypes.c_void_p()
+        rc = lib().pn_ens_create(ctypes.byref(h), len(systems), n, _p(e), ctypes.byref(self.params))
+        if rc != PN_OK:
+            raise PNError(rc, "pn_ens_create")
+        self._h = h
+        self.set_state(systems)
+
+    def _ck(self, rc, where):
+        if rc != PN_OK:
+            raise PNError(rc, where)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().pn_ens_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_state(self, systems):
+        x = np.ascontiguousarray(np.concatenate([s.x for s in systems]))
+        v = np.ascontiguousarray(np.concatenate([s.v for s in systems]))
+        m = np.ascontiguousarray(np.concatenate([s.m for s in systems]))
+        self._ck(lib().pn_ens_set_state(self._h, _p(x), _p(v), _p(m)), "pn_ens_set_state")
+
+    def split(self, arr):
+        return [arr[self.offsets[c]:self.offsets[c + 1]] for c in range(len(self.sizes))]
+
+    def get_state(self):
+        P = int(self.offsets[-1])
+        x = np.zeros((P, 3))
+        v = np.zeros((P, 3))
+        self._ck(lib().pn_ens_get_state(self._h, _p(x), _p(v)), "pn_ens_get_state")
+        return self.split(x), self.split(v)
+
+    def force(self):
+        a = np.zeros((int(self.offsets[-1]), 3))
+        self._ck(lib().pn_ens_force(self._h, _p(a)), "pn_ens_force")
+        return self.split(a)
+
+    def steps(self, k, sync=True):
+        self._ck(lib().pn_ens_steps(self._h, int(k)), "pn_ens_steps")
+        if sync:
+            self._ck(lib().pn_ens_sync(self._h), "pn_ens_sync")
+
+    def energy(self):
+        out = np.zeros(4 * len(self.sizes))
+        self._ck(lib().pn_ens_energy(self._h, _p(out)), "pn_ens_energy")
+        return out.reshape(-1, 4)
+
+    def bench_steps(self, k):
+        t = np.zeros(max(1, k))
+        self._ck(lib().pn_ens_bench_steps(self._h, int(k), _p(t)), "pn_ens_bench_steps")
+        return t[:k]
+
+    def autotune(self):
+        self._ck(lib().pn_ens_autotune(self._h), "pn_ens_autotune")
+
+    def set_shape(self, ipt=0, js=0, size_class=-1, tile_j=128, tiles_per_item=32):
+        self._ck(lib().pn_ens_set_shape(self._h, ipt, js, size_class, tile_j, tiles_per_item),
+                 "pn_ens_set_shape")
+
+    def shape(self, size_class):
+        v = [ctypes.c_int() for _ in range(4)]
+        self._ck(lib().pn_ens_get_shape(self._h, size_class, *[ctypes.byref(q) for q in v]),
+                 "pn_ens_get_shape")
+        return tuple(q.value for q in v)
 
 
 # ------------------------------------------------------------------ initial conditions and I/O

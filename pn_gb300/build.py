@@ -18,6 +18,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 OBJ = os.path.join(OUT, "obj")
 LIB = os.path.join(OUT, "libpn.so")
+CLI = os.path.join(HERE, "cli", "pn_run.c")
+EXE = os.path.join(OUT, "pn_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -79,6 +81,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
                 print(out)
     if force or jobs or _stale(LIB, objs):
         _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lm"])
+    if force or _stale(EXE, [CLI, LIB]):
+        # the command-line driver (the reference's main loop on the device-resident API)
+        _run(["gcc"] + CC_FLAGS + [CLI, "-L" + OUT, "-lpn", "-Wl,-rpath," + OUT, "-lm", "-o", EXE])
     return LIB
 
 

@@ -1,0 +1,783 @@
+// pn_adjoint.cu -- discrete adjoint of the force path and of the integration scheme.
+//
+// Force VJP.  For an adjoint abar (one 3-vector per particle) of the accelerations, the
+// gradients xbar, vbar of abar . a(x, v, m) and dL/dm0 are computed in four launches:
+//   k_prep            (forward, O(N)) pack and global sums of the evaluation state
+//   k_finish_vjp      (O(N)) per star: the adjoint of the closed forms of the finishing kernel
+//                     (generated from the same formulas, pn_finish_vjp_gen.cuh): adjoints of
+//                     the star's pair sums (the "adjoint state" Gbar, Phibar, S0bar, Ubar, Wbar),
+//                     of its own s, v, of the global sums and of m0
+//   k_pair_vjp        (O(N^2)) one symmetric sweep: for star p against every star q, the pair
+//                     term's derivative with p as the accumulating particle (adjoint state of p)
+//                     and with p as the source particle (adjoint state of q streamed with q's
+//                     data), i.e. the pairwise tidal-tensor contraction with the adjoint state
+//                     plus the hand-differentiated 1PN pair terms
+//   k_vjp_assemble    (O(N)) chain rule through R = (|s|^2+eps^2)^(-1/2), the per-particle
+//                     pack constants and the global sums; xbar_0 = -sum_p sbar_p; dL/dm0
+// The forward pair sums the VJP needs are those of the forward evaluation (stored by
+// k_finish's sums_out), so the O(N^2) forward sweep is not repeated.
+//
+// Trajectory adjoint.  pn_adj_forward runs nsteps integration steps and keeps the state every
+// K steps (checkpoints).  pn_adj_backward walks the segments backwards: each segment is
+// recomputed from its checkpoint, storing its stage states and pair sums, and then its steps are
+// reversed stage by stage (the adjoint of Limit-sticky9.c:853-891 is linear algebra on the
+// stage adjoints, with one force VJP per stage).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "pn_ctx.h"
+#include "pn_finish_vjp_gen.cuh"
+
+using namespace pn;
+
+namespace pn {
+
+enum VjpSlot : int { V_SX = 0, V_SY, V_SZ, V_VX, V_VY, V_VZ, V_QE, V_MU3, V_C1, V_C3, V_K35, NV_VJP };
+enum GbarSlot : int { GB_A1 = 0, GB_B3X, GB_B3Y, GB_B3Z, GB_C, GB_PX, GB_PY, GB_PZ, GB_M0, NGBAR };
+
+// ------------------------------------------------------------------ per-star adjoint
+struct FinVjpArgs {
+    const double *spos, *v, *m, *sums, *glob;
+    long long vsp, vsk;
+    const double *abar;  // [p*asp + k*ask]
+    long long asp, ask;
+    int nstar, npad, nfill, f32;
+    double eps, eps2, ic2;
+    void *apack;         // adjoint state per star (FP64: 5 double2 groups; FP32: 3 float4)
+    double *sdir, *vdir; // [3][npad]
+    double *part, *gbar;
+    unsigned *ticket;
+};
+
+__device__ __forceinline__ void block_sum_n(double *v, int nv, double *scratch) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int q = 0; q < nv; ++q)
+        for (int off = 16; off > 0; off >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], off);
+    if (lane == 0)
+        for (int q = 0; q < nv; ++q) scratch[warp * nv + q] = v[q];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int q = 0; q < nv; ++q) {
+            double s = 0.0;
+            for (int w = 0; w < nw; ++w) s += scratch[w * nv + q];
+            v[q] = s;
+        }
+    __syncthreads();
+}
+
+__device__ __forceinline__ bool last_of(unsigned *ticket) {
+    __shared__ bool am_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) am_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    return am_last;
+}
+
+__global__ void __launch_bounds__(256) k_finish_vjp(const FinVjpArgs a) {
+    __shared__ double red[32 * NGBAR];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double g[NGBAR];
+    for (int q = 0; q < NGBAR; ++q) g[q] = 0.0;
+    if (i < a.nfill) {
+        double Gb[3] = {0, 0, 0}, Wb[3] = {0, 0, 0}, Phib = 0, S0b = 0, Ub = 0;
+        if (i < a.nstar) {
+            const int p = i + 1;
+            const double s[3] = {a.spos[i], a.spos[a.npad + i], a.spos[2 * a.npad + i]};
+            double v[3], ab[3], bb[3], G[3];
+            for (int k = 0; k < 3; ++k) {
+                v[k] = a.v[p * a.vsp + k * a.vsk];
+                ab[k] = a.abar[p * a.asp + k * a.ask];
+                bb[k] = a.abar[k * a.ask];
+                G[k] = a.sums[(size_t)(A_GX + k) * a.npad + i];
+            }
+            const double Phi = a.sums[(size_t)A_PHI * a.npad + i];
+            const double S0 = a.sums[(size_t)A_S0 * a.npad + i];
+            const double U = a.sums[(size_t)A_U * a.npad + i];
+            double sb[3], vb[3], gBb[3], gPb[3], m0b, gAb, gCb;
+            finish_vjp_gen(s[0], s[1], s[2], v[0], v[1], v[2], G[0], G[1], G[2], a.glob[G_B3X],
+                           a.glob[G_B3Y], a.glob[G_B3Z], a.glob[G_PX], a.glob[G_PY], a.glob[G_PZ],
+                           ab[0], ab[1], ab[2], bb[0], bb[1], bb[2], Phi, S0, U, a.m[p], a.m[0],
+                           a.eps, a.eps2, a.ic2, a.glob[G_A1], a.glob[G_C], sb, vb, Gb, Wb, gBb, gPb,
+                           Phib, S0b, Ub, m0b, gAb, gCb);
+            for (int k = 0; k < 3; ++k) {
+                a.sdir[(size_t)k * a.npad + i] = sb[k];
+                a.vdir[(size_t)k * a.npad + i] = vb[k];
+            }
+            g[GB_A1] = gAb;
+            g[GB_C] = gCb;
+            g[GB_M0] = m0b;
+            for (int k = 0; k < 3; ++k) {
+                g[GB_B3X + k] = gBb[k];
+                g[GB_PX + k] = gPb[k];
+            }
+        }
+        if (a.f32) {
+            float4 *ap = static_cast<float4 *>(a.apack);
+            ap[i] = make_float4((float)Gb[0], (float)Gb[1], (float)Gb[2], (float)Phib);
+            ap[a.npad + i] = make_float4((float)Wb[0], (float)Wb[1], (float)Wb[2], (float)S0b);
+            ap[2 * a.npad + i] = make_float4((float)Ub, 0.f, 0.f, 0.f);
+        } else {
+            double2 *ap = static_cast<double2 *>(a.apack);
+            ap[i] = make_double2(Gb[0], Gb[1]);
+            ap[a.npad + i] = make_double2(Gb[2], Phib);
+            ap[2 * a.npad + i] = make_double2(S0b, Ub);
+            ap[3 * a.npad + i] = make_double2(Wb[0], Wb[1]);
+            ap[4 * a.npad + i] = make_double2(Wb[2], 0.0);
+        }
+    }
+    block_sum_n(g, NGBAR, red);
+    if (threadIdx.x == 0)
+        for (int q = 0; q < NGBAR; ++q) a.part[(size_t)blockIdx.x * NGBAR + q] = g[q];
+    if (last_of(a.ticket)) {
+        double t[NGBAR];
+        for (int q = 0; q < NGBAR; ++q) t[q] = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+            for (int q = 0; q < NGBAR; ++q) t[q] += __ldcg(&a.part[(size_t)b * NGBAR + q]);
+        block_sum_n(t, NGBAR, red);
+        if (threadIdx.x == 0) {
+            for (int q = 0; q < NGBAR; ++q) a.gbar[q] = t[q];
+            // the BH's Newtonian acceleration is B3 itself (Limit-sticky9.c:36-51, row 0)
+            for (int k = 0; k < 3; ++k) a.gbar[GB_B3X + k] += a.abar[k * a.ask];
+            *a.ticket = 0u;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ the O(N^2) adjoint sweep
+struct PairVjpArgs {
+    const void *pack;    // forward pack (prep), [NGF][npad]
+    const void *apack;   // adjoint state, [NGA][npad]
+    const TileOrigin *torg;
+    const double *spos;
+    double *out;         // [gsplit][NV_VJP][npad]
+    int *err;
+    int nstar, npad, tj, ntiles, gsplit;
+    double eps2;
+};
+
+template <typename T> struct VjpState {
+    T ex, ey, ez, lx, ly, lz;  // position (FP32: hi/lo relative to the tile origin)
+    T vx, vy, vz, vi2, m, mu3, c1, c3, k35, qe;
+    T Gx, Gy, Gz, Phi, S0, U, Wx, Wy, Wz;  // adjoint state
+};
+
+// One (p, q) pair, both roles.  d = s_q - s_p.  Accumulates into acc[NV_VJP] of p.
+template <typename T>
+__device__ __forceinline__ void vjp_pair(T *acc, const VjpState<T> &P, const VjpState<T> &Qj, T dx, T dy,
+                                         T dz, T eps2) {
+    const T rhoe = pn_fma(dz, dz, pn_fma(dy, dy, pn_fma(dx, dx, eps2)));
+    const T Q = pn_rsqrt<T>(rhoe);
+    const T Q2 = Q * Q, Q3 = Q2 * Q;
+    const T dvx = Qj.vx - P.vx, dvy = Qj.vy - P.vy, dvz = Qj.vz - P.vz;
+    const T dv2 = dvx * dvx + dvy * dvy + dvz * dvz;
+    const T vdp = P.vx * dx + P.vy * dy + P.vz * dz;   // v_p . d
+    const T vdq = Qj.vx * dx + Qj.vy * dy + Qj.vz * dz;  // v_q . d
+    // ---- p accumulates (i = p, j = q), adjoint state of p; d = s_j - s_i
+    {
+        const T mQ3 = Qj.m * Q3;
+        const T gd = P.Gx * dx + P.Gy * dy + P.Gz * dz;
+        const T wd = P.Wx * dx + P.Wy * dy + P.Wz * dz;
+        const T wdv = P.Wx * dvx + P.Wy * dvy + P.Wz * dvz;
+        const T br = Qj.c1 + Qj.c3 * (rhoe - P.qe) + P.vi2 - T(2) * dv2 + T(1.5) * vdq * vdq * Q2;
+        const T k4 = T(4) * vdp - T(3) * vdq;
+        const T cd = mQ3 * br + Qj.k35 * Q;
+        const T cv = mQ3 * k4;
+        const T LQ = T(3) * Qj.m * Q2 * (gd + P.S0 + br * wd + k4 * wdv) + P.Phi * Qj.m + P.U * Qj.mu3 +
+                     wd * (T(3) * mQ3 * vdq * vdq * Q + Qj.k35);
+        const T e2 = T(2) * Qj.c3 * wd, e3 = T(3) * Q2 * vdq * wd;
+        const T Dx = mQ3 * (P.Gx + e2 * dx + e3 * Qj.vx + wdv * (T(4) * P.vx - T(3) * Qj.vx)) + cd * P.Wx - LQ * Q3 * dx;
+        const T Dy = mQ3 * (P.Gy + e2 * dy + e3 * Qj.vy + wdv * (T(4) * P.vy - T(3) * Qj.vy)) + cd * P.Wy - LQ * Q3 * dy;
+        const T Dz = mQ3 * (P.Gz + e2 * dz + e3 * Qj.vz + wdv * (T(4) * P.vz - T(3) * Qj.vz)) + cd * P.Wz - LQ * Q3 * dz;
+        acc[V_SX] -= Dx;
+        acc[V_SY] -= Dy;
+        acc[V_SZ] -= Dz;
+        const T f4 = T(4) * mQ3 * wdv;
+        acc[V_VX] += mQ3 * wd * (T(2) * P.vx + T(4) * dvx) + f4 * dx - cv * P.Wx;
+        acc[V_VY] += mQ3 * wd * (T(2) * P.vy + T(4) * dvy) + f4 * dy - cv * P.Wy;
+        acc[V_VZ] += mQ3 * wd * (T(2) * P.vz + T(4) * dvz) + f4 * dz - cv * P.Wz;
+        acc[V_QE] -= Qj.c3 * mQ3 * wd;
+    }
+    // ---- p is the source (i = q, j = p), adjoint state of q; d' = s_p - s_q = -d
+    {
+        const T ex = -dx, ey = -dy, ez = -dz;   // d'
+        const T fx = -dvx, fy = -dvy, fz = -dvz;  // dv' = v_p - v_q
+        const T mQ3 = P.m * Q3;
+        const T gd = Qj.Gx * ex + Qj.Gy * ey + Qj.Gz * ez;
+        const T wd = Qj.Wx * ex + Qj.Wy * ey + Qj.Wz * ez;
+        const T wdv = Qj.Wx * fx + Qj.Wy * fy + Qj.Wz * fz;
+        const T vdj = -vdp, vdi = -vdq;  // v_j . d', v_i . d'
+        const T rq = rhoe - Qj.qe;
+        const T br = P.c1 + P.c3 * rq + Qj.vi2 - T(2) * dv2 + T(1.5) * vdj * vdj * Q2;
+        const T k4 = T(4) * vdi - T(3) * vdj;
+        const T cd = mQ3 * br + P.k35 * Q;
+        const T cv = mQ3 * k4;
+        const T LQ = T(3) * P.m * Q2 * (gd + Qj.S0 + br * wd + k4 * wdv) + Qj.Phi * P.m + Qj.U * P.mu3 +
+                     wd * (T(3) * mQ3 * vdj * vdj * Q + P.k35);
+        const T e2 = T(2) * P.c3 * wd, e3 = T(3) * Q2 * vdj * wd;
+        const T Dx = mQ3 * (Qj.Gx + e2 * ex + e3 * P.vx + wdv * (T(4) * Qj.vx - T(3) * P.vx)) + cd * Qj.Wx - LQ * Q3 * ex;
+        const T Dy = mQ3 * (Qj.Gy + e2 * ey + e3 * P.vy + wdv * (T(4) * Qj.vy - T(3) * P.vy)) + cd * Qj.Wy - LQ * Q3 * ey;
+        const T Dz = mQ3 * (Qj.Gz + e2 * ez + e3 * P.vz + wdv * (T(4) * Qj.vz - T(3) * P.vz)) + cd * Qj.Wz - LQ * Q3 * ez;
+        acc[V_SX] += Dx;
+        acc[V_SY] += Dy;
+        acc[V_SZ] += Dz;
+        const T g3 = T(3) * Q2 * vdj;
+        acc[V_VX] += mQ3 * wd * (T(-4) * fx + g3 * ex) - T(3) * wdv * mQ3 * ex + cv * Qj.Wx;
+        acc[V_VY] += mQ3 * wd * (T(-4) * fy + g3 * ey) - T(3) * wdv * mQ3 * ey + cv * Qj.Wy;
+        acc[V_VZ] += mQ3 * wd * (T(-4) * fz + g3 * ez) - T(3) * wdv * mQ3 * ez + cv * Qj.Wz;
+        acc[V_MU3] += Qj.U * Q;
+        const T mw = mQ3 * wd;
+        acc[V_C1] += mw;
+        acc[V_C3] += mw * rq;
+        acc[V_K35] += Q * wd;
+    }
+}
+
+template <typename T> struct VjpPack;
+template <> struct VjpPack<float> { using V = float4; static constexpr int NGF = 4, NGA = 3; };
+template <> struct VjpPack<double> { using V = double2; static constexpr int NGF = 6, NGA = 5; };
+
+template <typename T>
+__device__ __forceinline__ void vjp_load(VjpState<T> &S, const typename VjpPack<T>::V *f, const typename VjpPack<T>::V *ad,
+                                         int stride, int j) {
+    if constexpr (sizeof(T) == 4) {
+        const float4 g0 = f[j], g1 = f[stride + j], g2 = f[2 * stride + j], g3 = f[3 * stride + j];
+        S.ex = g0.x; S.ey = g0.y; S.ez = g0.z; S.m = g0.w;
+        S.lx = g1.x; S.ly = g1.y; S.lz = g1.z; S.mu3 = g1.w;
+        S.vx = g2.x; S.vy = g2.y; S.vz = g2.z; S.qe = g2.w;
+        S.c1 = g3.x; S.c3 = g3.y; S.k35 = g3.z;
+        const float4 a0 = ad[j], a1 = ad[stride + j], a2 = ad[2 * stride + j];
+        S.Gx = a0.x; S.Gy = a0.y; S.Gz = a0.z; S.Phi = a0.w;
+        S.Wx = a1.x; S.Wy = a1.y; S.Wz = a1.z; S.S0 = a1.w;
+        S.U = a2.x;
+    } else {
+        const double2 g0 = f[j], g1 = f[stride + j], g2 = f[2 * stride + j], g3 = f[3 * stride + j],
+                      g4 = f[4 * stride + j], g5 = f[5 * stride + j];
+        S.ex = g0.x; S.ey = g0.y; S.ez = g1.x; S.m = g1.y;
+        S.lx = S.ly = S.lz = 0.0;
+        S.vx = g2.x; S.vy = g2.y; S.vz = g3.x; S.mu3 = g3.y;
+        S.c1 = g4.x; S.c3 = g4.y; S.k35 = g5.x; S.qe = g5.y;
+        const double2 a0 = ad[j], a1 = ad[stride + j], a2 = ad[2 * stride + j], a3 = ad[3 * stride + j],
+                      a4 = ad[4 * stride + j];
+        S.Gx = a0.x; S.Gy = a0.y; S.Gz = a1.x; S.Phi = a1.y;
+        S.S0 = a2.x; S.U = a2.y;
+        S.Wx = a3.x; S.Wy = a3.y; S.Wz = a4.x;
+    }
+    S.vi2 = S.vx * S.vx + S.vy * S.vy + S.vz * S.vz;
+}
+
+constexpr int VJP_NT = 128;
+
+// One thread per star p, tiles of tj stars q staged by the TMA engine (double buffered), the
+// j-range split over gridDim.y; FP32 sums are Kahan-folded per tile.
+template <typename T>
+__global__ void __launch_bounds__(VJP_NT) k_pair_vjp(const PairVjpArgs a) {
+    using V = typename VjpPack<T>::V;
+    constexpr int NGF = VjpPack<T>::NGF, NGA = VjpPack<T>::NGA, NG = NGF + NGA;
+    constexpr bool F32 = sizeof(T) == 4;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    V *buf = reinterpret_cast<V *>(smem + 128);
+    const int tid = threadIdx.x;
+    const int i = blockIdx.x * VJP_NT + tid;
+    const int split = blockIdx.y;
+    const int t0 = (int)(((long long)a.ntiles * split) / a.gsplit);
+    const int t1 = (int)(((long long)a.ntiles * (split + 1)) / a.gsplit);
+    const int tj = a.tj;
+    const V *pf = static_cast<const V *>(a.pack);
+    const V *pa = static_cast<const V *>(a.apack);
+    const bool valid = i < a.nstar;
+    VjpState<T> P{};
+    double sx = 0, sy = 0, sz = 0;
+    if (valid) {
+        vjp_load<T>(P, pf, pa, a.npad, i);
+        sx = a.spos[i];
+        sy = a.spos[a.npad + i];
+        sz = a.spos[2 * a.npad + i];
+        P.ex = (T)sx; P.ey = (T)sy; P.ez = (T)sz;
+        P.lx = P.ly = P.lz = T(0);
+    }
+    T run[NV_VJP], cmp[NV_VJP];
+    for (int q = 0; q < NV_VJP; ++q) run[q] = cmp[q] = T(0);
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const uint32_t gbytes = (uint32_t)tj * (uint32_t)sizeof(V);
+    auto issue = [&](int t, int stage) {
+        mbar_arrive_expect_tx(&bars[stage], (uint32_t)NG * gbytes);
+        for (int g = 0; g < NGF; ++g)
+            bulk_g2s(buf + (size_t)(stage * NG + g) * tj, pf + (size_t)g * a.npad + (size_t)t * tj, gbytes, &bars[stage]);
+        for (int g = 0; g < NGA; ++g)
+            bulk_g2s(buf + (size_t)(stage * NG + NGF + g) * tj, pa + (size_t)g * a.npad + (size_t)t * tj, gbytes,
+                     &bars[stage]);
+    };
+    if (tid == 0 && t0 < t1) issue(t0, 0);
+    for (int t = t0; t < t1; ++t) {
+        const int it = t - t0, stage = it & 1;
+        const uint32_t phase = (uint32_t)(it >> 1) & 1u;
+        const bool next = t + 1 < t1;
+        if (tid == 0 && next) issue(t + 1, stage ^ 1);
+        const bool ok = mbar_wait_bounded(&bars[stage], phase);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicOr(a.err, DEVERR_TIMEOUT);
+                mbar_wait_bounded(&bars[stage], phase);
+                if (next) mbar_wait_bounded(&bars[stage ^ 1], (uint32_t)((it + 1) >> 1) & 1u);
+            }
+            return;
+        }
+        if constexpr (F32) {
+            const TileOrigin o = a.torg[t];
+            const double rx = sx - o.x, ry = sy - o.y, rz = sz - o.z;
+            P.ex = (float)rx; P.ey = (float)ry; P.ez = (float)rz;
+            P.lx = (float)(rx - (double)P.ex); P.ly = (float)(ry - (double)P.ey); P.lz = (float)(rz - (double)P.ez);
+        }
+        const V *bf = buf + (size_t)stage * NG * tj;
+        const V *ba = bf + (size_t)NGF * tj;
+        T tacc[NV_VJP];
+        for (int q = 0; q < NV_VJP; ++q) tacc[q] = T(0);
+        for (int j = 0; j < tj; ++j) {
+            VjpState<T> Qj;
+            vjp_load<T>(Qj, bf, ba, tj, j);
+            T dx, dy, dz;
+            if constexpr (F32) {
+                dx = (Qj.ex - P.ex) + (Qj.lx - P.lx);
+                dy = (Qj.ey - P.ey) + (Qj.ly - P.ly);
+                dz = (Qj.ez - P.ez) + (Qj.lz - P.lz);
+            } else {
+                dx = Qj.ex - P.ex;
+                dy = Qj.ey - P.ey;
+                dz = Qj.ez - P.ez;
+            }
+            vjp_pair<T>(F32 ? tacc : run, P, Qj, dx, dy, dz, (T)a.eps2);
+        }
+        if constexpr (F32)
+            for (int q = 0; q < NV_VJP; ++q) kahan_add(run[q], cmp[q], tacc[q]);
+        __syncthreads();
+    }
+    if (valid)
+        for (int q = 0; q < NV_VJP; ++q)
+            a.out[((size_t)split * NV_VJP + q) * a.npad + i] = F32 ? (double)run[q] - (double)cmp[q] : (double)run[q];
+}
+
+// ------------------------------------------------------------------ assembly
+struct AssembleArgs {
+    const double *spos, *m, *vjp, *sdir, *vdir, *gbar;
+    int nstar, npad, gsplit;
+    double eps2;
+    double *xbar, *vbar;  // outputs [p*osp + k*osk] (accumulated into when accumulate != 0)
+    long long osp, osk;
+    int accumulate;
+    int m0_accumulate;
+    double *part, *m0bar;  // m0bar[0] += dL/dm0 (when m0_accumulate) or = (otherwise)
+    unsigned *ticket;
+};
+
+__global__ void __launch_bounds__(256) k_vjp_assemble(const AssembleArgs a) {
+    __shared__ double red[32 * 4];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double r[4] = {0, 0, 0, 0};  // -sum sbar (3), m0 partial
+    if (i < a.nstar) {
+        const int p = i + 1;
+        const double s[3] = {a.spos[i], a.spos[a.npad + i], a.spos[2 * a.npad + i]};
+        double S[NV_VJP];
+        for (int q = 0; q < NV_VJP; ++q) {
+            double t = 0.0;
+            for (int g = 0; g < a.gsplit; ++g) t += a.vjp[((size_t)g * NV_VJP + q) * a.npad + i];
+            S[q] = t;
+        }
+        const double mp = a.m[p], m0 = a.m[0];
+        const double q2 = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
+        const double R = 1.0 / sqrt(q2 + a.eps2), R2 = R * R, R3 = R2 * R;
+        const double *G = a.gbar;
+        const double B3s = G[GB_B3X] * s[0] + G[GB_B3Y] * s[1] + G[GB_B3Z] * s[2];
+        // R enters c1 = 1.25 m0 R, c3 = 0.25 m0 R^3, k35 = 3.5 m0 m R^3, mu3 = m R^3 (pack) and
+        // A1 = sum m R, B3 = sum m R^3 s, C = sum m R^3 q (global sums)
+        const double Rb = 1.25 * m0 * S[V_C1] + 0.75 * m0 * R2 * S[V_C3] + 10.5 * m0 * mp * R2 * S[V_K35] +
+                          3.0 * mp * R2 * S[V_MU3] + mp * G[GB_A1] + 3.0 * mp * R2 * B3s +
+                          3.0 * mp * R2 * q2 * G[GB_C];
+        const double qb = S[V_QE] + G[GB_C] * mp * R3;
+        double sb[3], vb[3];
+        for (int k = 0; k < 3; ++k) {
+            sb[k] = a.sdir[(size_t)k * a.npad + i] + S[V_SX + k] - Rb * R3 * s[k] + 2.0 * qb * s[k] +
+                    G[GB_B3X + k] * mp * R3;
+            vb[k] = a.vdir[(size_t)k * a.npad + i] + S[V_VX + k] + mp * G[GB_PX + k];
+            double *xo = &a.xbar[p * a.osp + k * a.osk];
+            double *vo = &a.vbar[p * a.osp + k * a.osk];
+            *xo = a.accumulate ? *xo + sb[k] : sb[k];
+            *vo = a.accumulate ? *vo + vb[k] : vb[k];
+            r[k] = -sb[k];
+        }
+        r[3] = 1.25 * R * S[V_C1] + 0.25 * R3 * S[V_C3] + 3.5 * mp * R3 * S[V_K35];
+    }
+    block_sum_n(r, 4, red);
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 4; ++q) a.part[(size_t)blockIdx.x * 4 + q] = r[q];
+    if (last_of(a.ticket)) {
+        double t[4] = {0, 0, 0, 0};
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+            for (int q = 0; q < 4; ++q) t[q] += __ldcg(&a.part[(size_t)b * 4 + q]);
+        block_sum_n(t, 4, red);
+        if (threadIdx.x == 0) {
+            for (int k = 0; k < 3; ++k) {
+                double *xo = &a.xbar[k * a.osk];
+                double *vo = &a.vbar[k * a.osk];
+                *xo = a.accumulate ? *xo + t[k] : t[k];  // x_0 enters through s_p = x_p - x_0
+                if (!a.accumulate) *vo = 0.0;             // the force ignores the BH velocity
+            }
+            const double m0b = t[3] + a.gbar[GB_M0];
+            a.m0bar[0] = a.m0_accumulate ? a.m0bar[0] + m0b : m0b;
+            *a.ticket = 0u;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ integrator adjoint (elementwise)
+// Reverse of one step (Limit-sticky9.c:853-891): called with which = 0..4.
+//   0: from (Xb, Vb): xb = Xb/6, vb = Vb/6; x3b = Xb/6, x1b = x2b = Xb/3; v3b = Vb/6, v1b = v2b = Vb/3;
+//      then x3 = x + h v2, v3 = v + h a2: xb += x3b, v2b += h x3b, vb += v3b, ab = h v3b
+//   1: after the VJP at (x2, v2): xb += x2b, v1b += h/2 x2b, vb += v2b, ab = h/2 v2b
+//   2: after the VJP at (x1, v1): xb += x1b, vb += h/2 x1b + v1b, ab = h/2 v1b
+// The VJP outputs (xF, vF) are added to (x2b, v2b), (x1b, v1b), (xb, vb) respectively.
+struct StageAdjArgs {
+    double *Xb, *Vb;   // in: step-output adjoints; out (which 3): step-input adjoints
+    double *xb, *vb, *x1b, *v1b, *x2b, *v2b, *ab;
+    const double *xF, *vF;
+    double h;
+    int n;
+    long long ld;
+    int which;
+};
+
+__global__ void k_stage_adj(const StageAdjArgs a) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.n) return;
+    for (int k = 0; k < 3; ++k) {
+        const size_t o = (size_t)k * a.ld + p;
+        const double h = a.h;
+        if (a.which == 0) {
+            const double X = a.Xb[o], Vv = a.Vb[o];
+            const double x3b = X / 6.0, v3b = Vv / 6.0;
+            a.xb[o] = X / 6.0 + x3b;
+            a.x1b[o] = X / 3.0;
+            a.x2b[o] = X / 3.0;
+            a.v1b[o] = Vv / 3.0;
+            a.v2b[o] = Vv / 3.0 + h * x3b;
+            a.vb[o] = Vv / 6.0 + v3b;
+            a.ab[o] = h * v3b;
+        } else if (a.which == 1) {  // VJP at (x2, v2) done: add it, then reverse x2, v2
+            const double x2b = a.x2b[o] + a.xF[o], v2b = a.v2b[o] + a.vF[o];
+            a.xb[o] += x2b;
+            a.v1b[o] += 0.5 * h * x2b;
+            a.vb[o] += v2b;
+            a.ab[o] = 0.5 * h * v2b;
+        } else if (a.which == 2) {  // VJP at (x1, v1) done: add it, then reverse x1, v1
+            const double x1b = a.x1b[o] + a.xF[o], v1b = a.v1b[o] + a.vF[o];
+            a.xb[o] += x1b;
+            a.vb[o] += 0.5 * h * x1b + v1b;
+            a.ab[o] = 0.5 * h * v1b;
+        } else {  // VJP at (x, v) done: the step-input adjoints
+            a.Xb[o] = a.xb[o] + a.xF[o];
+            a.Vb[o] = a.vb[o] + a.vF[o];
+        }
+    }
+}
+
+}  // namespace pn
+
+// ------------------------------------------------------------------ host side
+struct AdjointWork {
+    int npad = 0;
+    long long ld = 0;
+    double *sums = nullptr;  // [9][npad]
+    void *apack = nullptr;   // [5][npad] x 16 B
+    double *sdir = nullptr, *vdir = nullptr, *vjp = nullptr, *gbar = nullptr, *part = nullptr;
+    int vjp_splits = 0;
+    double *m0bar = nullptr;
+    unsigned *tickets = nullptr;
+    double *work = nullptr;  // [12][3][ld]: Xb Vb xb vb x1b v1b x2b v2b ab xF vF spare
+    // trajectory
+    int nsteps = 0, K = 0, nck = 0;
+    double *ckpt = nullptr;     // [nck][6][ld]  (x, v at steps 0, K, 2K, ...)
+    double *seg = nullptr;      // [K][3][6][ld] evaluation states of a segment's stages
+    double *segsums = nullptr;  // [K][3][9][npad]
+    double time0 = 0.0;
+};
+
+namespace pn {
+
+void free_adjoint(pn_ctx *c) {
+    AdjointWork *w = c->adj;
+    if (!w) return;
+    void *b[] = {w->sums, w->apack, w->sdir, w->vdir, w->vjp, w->gbar, w->part, w->m0bar, w->tickets,
+                 w->work, w->ckpt, w->seg, w->segsums};
+    for (void *p : b)
+        if (p) cudaFree(p);
+    delete w;
+    c->adj = nullptr;
+}
+
+}  // namespace pn
+
+static int adj_ensure(pn_ctx *c) {
+    if (c->adj) return PN_OK;
+    AdjointWork *w = new AdjointWork();
+    c->adj = w;
+    w->npad = c->npad;
+    w->ld = c->ld;
+    const size_t np = (size_t)c->npad, ld = (size_t)c->ld;
+    auto mal = [&](void **p, size_t bytes) {
+        if (cudaMalloc(p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        return true;
+    };
+    const bool ok = mal((void **)&w->sums, 9 * np * 8) && mal(&w->apack, 5 * np * 16) &&
+                    mal((void **)&w->sdir, 3 * np * 8) && mal((void **)&w->vdir, 3 * np * 8) &&
+                    mal((void **)&w->gbar, 16 * 8) && mal((void **)&w->part, (np / 256 + 2) * 16 * 8) &&
+                    mal((void **)&w->m0bar, 2 * 8) && mal((void **)&w->tickets, 4 * sizeof(unsigned)) &&
+                    mal((void **)&w->work, 12 * 3 * ld * 8);
+    if (!ok) {
+        free_adjoint(c);
+        return set_err(PN_ERR_NOMEM, "adjoint buffers");
+    }
+    CU(cudaMemset(w->tickets, 0, 4 * sizeof(unsigned)));
+    CU(cudaMemset(w->apack, 0, 5 * np * 16));
+    CU(cudaMemset(w->work, 0, 12 * 3 * ld * 8));
+    return PN_OK;
+}
+
+static int vjp_tj(const pn_ctx *c) { return is_f32(c) ? 128 : 64; }
+
+// VJP of one force evaluation at (x, v) (SoA, leading dim ld), whose pair sums are in `sums`
+// ([9][npad]).  abar: SoA [3][ld].  Writes (accumulate=0) or adds (1) xbar, vbar (SoA) and
+// m0bar.
+static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *sums, const double *abar,
+                    double *xbar, double *vbar, double *m0bar, int m0_accumulate, cudaStream_t s) {
+    const int accumulate = 0;
+    AdjointWork *w = c->adj;
+    const int nstar = c->n - 1;
+    const bool f32 = is_f32(c);
+    const int tj = vjp_tj(c);
+    const double eps2 = c->p.eps * c->p.eps;
+    const long long ld = c->ld;
+    // prep: pack (forward data), global sums of this state
+    PrepArgs pa{};
+    pa.x = x; pa.v = v; pa.m = c->st.m; pa.sp = 1; pa.sk = ld;
+    pa.nstar = nstar; pa.npad = c->npad; pa.nfill = (int)round_up(nstar > 0 ? nstar : 1, 256);
+    pa.tj = tj; pa.f32 = f32; pa.eps2 = eps2;
+    pa.pack = c->pack; pa.torg = c->torg; pa.spos = c->spos;
+    pa.part = c->part; pa.glob = c->glob; pa.ticket = &c->tickets[0];
+    CU(launch_prep(pa, s));
+    // per-star adjoint
+    FinVjpArgs fa{};
+    fa.spos = c->spos; fa.v = v; fa.m = c->st.m; fa.sums = sums; fa.glob = c->glob;
+    fa.vsp = 1; fa.vsk = ld; fa.abar = abar; fa.asp = 1; fa.ask = ld;
+    fa.nstar = nstar; fa.npad = c->npad; fa.nfill = pa.nfill; fa.f32 = f32;
+    fa.eps = c->p.eps; fa.eps2 = eps2; fa.ic2 = c->p.inv_c2;
+    fa.apack = w->apack; fa.sdir = w->sdir; fa.vdir = w->vdir; fa.part = w->part; fa.gbar = w->gbar;
+    fa.ticket = &w->tickets[0];
+    const int nbf = (pa.nfill + 255) / 256;
+    k_finish_vjp<<<nbf, 256, 0, s>>>(fa);
+    CU(cudaGetLastError());
+    // O(N^2) sweep
+    const int ntiles = nstar > 0 ? (nstar + tj - 1) / tj : 0;
+    const int nib = (nstar + VJP_NT - 1) / VJP_NT;
+    int g = nib > 0 ? (4 * 152 * 6 + nib - 1) / nib : 1;
+    if (g > 32) g = 32;
+    if (g > ntiles) g = ntiles;
+    if (g < 1) g = 1;
+    if (g > w->vjp_splits) {
+        if (w->vjp) cudaFree(w->vjp);
+        w->vjp = nullptr;
+        if (cudaMalloc(&w->vjp, (size_t)g * NV_VJP * c->npad * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            w->vjp_splits = 0;
+            return set_err(PN_ERR_NOMEM, "vjp partials");
+        }
+        w->vjp_splits = g;
+    }
+    if (nstar > 0) {
+        PairVjpArgs qa{};
+        qa.pack = c->pack; qa.apack = w->apack; qa.torg = c->torg; qa.spos = c->spos; qa.out = w->vjp;
+        qa.err = c->err; qa.nstar = nstar; qa.npad = c->npad; qa.tj = tj; qa.ntiles = ntiles; qa.gsplit = g;
+        qa.eps2 = eps2;
+        dim3 grid((unsigned)nib, (unsigned)g);
+        if (f32) {
+            const size_t smem = 128 + 2 * (size_t)(4 + 3) * tj * 16;
+            k_pair_vjp<float><<<grid, VJP_NT, smem, s>>>(qa);
+        } else {
+            const size_t smem = 128 + 2 * (size_t)(6 + 5) * tj * 16;
+            k_pair_vjp<double><<<grid, VJP_NT, smem, s>>>(qa);
+        }
+        CU(cudaGetLastError());
+    }
+    AssembleArgs aa{};
+    aa.spos = c->spos; aa.m = c->st.m; aa.vjp = w->vjp; aa.sdir = w->sdir; aa.vdir = w->vdir; aa.gbar = w->gbar;
+    aa.nstar = nstar; aa.npad = c->npad; aa.gsplit = nstar > 0 ? g : 0; aa.eps2 = eps2;
+    aa.xbar = xbar; aa.vbar = vbar; aa.osp = 1; aa.osk = ld; aa.accumulate = accumulate;
+    aa.m0_accumulate = m0_accumulate;
+    aa.part = w->part; aa.m0bar = m0bar; aa.ticket = &w->tickets[1];
+    const int nba = nstar > 0 ? (nstar + 255) / 256 : 1;
+    k_vjp_assemble<<<nba, 256, 0, s>>>(aa);
+    CU(cudaGetLastError());
+    return PN_OK;
+}
+
+static void to_soa(const double *aos, double *h, int n, size_t ld) {
+    for (int p = 0; p < n; ++p)
+        for (int k = 0; k < 3; ++k) h[k * ld + p] = aos[3 * p + k];
+}
+static void from_soa(const double *h, double *aos, int n, size_t ld) {
+    for (int p = 0; p < n; ++p)
+        for (int k = 0; k < 3; ++k) aos[3 * p + k] = h[k * ld + p];
+}
+
+extern "C" int pn_force_vjp(pn_ctx *c, const double *abar, double *xbar, double *vbar, double *m0bar) {
+    if (!c || !c->have_state) return set_err(PN_ERR_STATE, "pn_force_vjp: no state");
+    if (!abar || !xbar || !vbar || !m0bar) return set_err(PN_ERR_INVALID, "pn_force_vjp");
+    int rc = adj_ensure(c);
+    if (rc) return rc;
+    AdjointWork *w = c->adj;
+    const size_t ld = (size_t)c->ld;
+    cudaStream_t s = c->stream;
+    // forward evaluation (its pair sums feed the VJP)
+    rc = eval_force(c, c->st.x, c->st.v, c->st.m, 1, c->ld, nullptr, 3, 1, 0, s, false, -1, w->sums);
+    if (rc) return rc;
+    std::vector<double> h(3 * ld, 0.0);
+    to_soa(abar, h.data(), c->n, ld);
+    double *d_ab = w->work + 8 * 3 * ld, *d_xF = w->work + 9 * 3 * ld, *d_vF = w->work + 10 * 3 * ld;
+    CU(cudaMemcpyAsync(d_ab, h.data(), 3 * ld * 8, cudaMemcpyHostToDevice, s));
+    rc = vjp_eval(c, c->st.x, c->st.v, w->sums, d_ab, d_xF, d_vF, w->m0bar, 0, s);
+    if (rc) return rc;
+    std::vector<double> hx(3 * ld), hv(3 * ld);
+    CU(cudaMemcpyAsync(hx.data(), d_xF, 3 * ld * 8, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(hv.data(), d_vF, 3 * ld * 8, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(m0bar, w->m0bar, 8, cudaMemcpyDeviceToHost, s));
+    rc = check_device_err(c);
+    if (rc) return rc;
+    from_soa(hx.data(), xbar, c->n, ld);
+    from_soa(hv.data(), vbar, c->n, ld);
+    return PN_OK;
+}
+
+extern "C" int pn_adj_forward(pn_ctx *c, int nsteps, int checkpoint_every) {
+    if (!c || !c->have_state) return set_err(PN_ERR_STATE, "pn_adj_forward: no state");
+    if (nsteps < 1 || checkpoint_every < 1) return set_err(PN_ERR_INVALID, "pn_adj_forward");
+    int rc = adj_ensure(c);
+    if (rc) return rc;
+    AdjointWork *w = c->adj;
+    const size_t ld = (size_t)c->ld, np = (size_t)c->npad;
+    const int K = checkpoint_every;
+    const int nck = (nsteps + K - 1) / K;
+    if (w->nsteps != nsteps || w->K != K) {
+        if (w->ckpt) cudaFree(w->ckpt);
+        if (w->seg) cudaFree(w->seg);
+        if (w->segsums) cudaFree(w->segsums);
+        w->ckpt = w->seg = w->segsums = nullptr;
+        if (cudaMalloc(&w->ckpt, (size_t)nck * 6 * ld * 8) != cudaSuccess ||
+            cudaMalloc(&w->seg, (size_t)K * 3 * 6 * ld * 8) != cudaSuccess ||
+            cudaMalloc(&w->segsums, (size_t)K * 3 * 9 * np * 8) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(PN_ERR_NOMEM, "checkpoints");
+        }
+        w->nsteps = nsteps;
+        w->K = K;
+        w->nck = nck;
+    }
+    w->time0 = c->time;
+    for (int k = 0; k < nck; ++k) {
+        CU(cudaMemcpyAsync(w->ckpt + (size_t)k * 6 * ld, c->st.x, 6 * ld * 8, cudaMemcpyDeviceToDevice, c->stream));
+        const int steps = (k + 1) * K <= nsteps ? K : nsteps - k * K;
+        rc = pn_steps(c, steps);
+        if (rc) return rc;
+    }
+    return check_device_err(c);
+}
+
+extern "C" int pn_adj_backward(pn_ctx *c, const double *xbar_T, const double *vbar_T, double *xbar_0,
+                               double *vbar_0, double *m0bar) {
+    if (!c || !c->adj || !c->adj->ckpt) return set_err(PN_ERR_STATE, "pn_adj_backward: no forward run");
+    if (!xbar_T || !vbar_T || !xbar_0 || !vbar_0 || !m0bar) return set_err(PN_ERR_INVALID, "pn_adj_backward");
+    AdjointWork *w = c->adj;
+    const size_t ld = (size_t)c->ld, np = (size_t)c->npad;
+    const long long LD = c->ld;
+    cudaStream_t s = c->stream;
+    const double h = c->p.dt;
+    double *Xb = w->work, *Vb = w->work + 3 * ld, *xb = w->work + 2 * 3 * ld, *vb = w->work + 3 * 3 * ld;
+    double *x1b = w->work + 4 * 3 * ld, *v1b = w->work + 5 * 3 * ld, *x2b = w->work + 6 * 3 * ld;
+    double *v2b = w->work + 7 * 3 * ld, *ab = w->work + 8 * 3 * ld, *xF = w->work + 9 * 3 * ld;
+    double *vF = w->work + 10 * 3 * ld;
+    std::vector<double> hb(6 * ld, 0.0);
+    to_soa(xbar_T, hb.data(), c->n, ld);
+    to_soa(vbar_T, hb.data() + 3 * ld, c->n, ld);
+    CU(cudaMemcpyAsync(Xb, hb.data(), 6 * ld * 8, cudaMemcpyHostToDevice, s));  // Xb, Vb adjacent
+    CU(cudaMemsetAsync(w->m0bar + 1, 0, 8, s));
+    // the context's state arrays are the recompute workspace; the final state is restored last
+    std::vector<double> final_state(6 * ld);
+    CU(cudaMemcpyAsync(final_state.data(), c->st.x, 6 * ld * 8, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    const int nthreads = 256, nblk = (c->n + nthreads - 1) / nthreads;
+    StageAdjArgs sa{};
+    sa.Xb = Xb; sa.Vb = Vb; sa.xb = xb; sa.vb = vb; sa.x1b = x1b; sa.v1b = v1b; sa.x2b = x2b; sa.v2b = v2b;
+    sa.ab = ab; sa.xF = xF; sa.vF = vF; sa.h = h; sa.n = c->n; sa.ld = LD;
+    for (int k = w->nck - 1; k >= 0; --k) {
+        const int steps = (k + 1) * w->K <= w->nsteps ? w->K : w->nsteps - k * w->K;
+        // recompute the segment, keeping every stage's evaluation state and pair sums
+        CU(cudaMemcpyAsync(c->st.x, w->ckpt + (size_t)k * 6 * ld, 6 * ld * 8, cudaMemcpyDeviceToDevice, s));
+        for (int t = 0; t < steps; ++t) {
+            double *S0 = w->seg + ((size_t)t * 3 + 0) * 6 * ld;
+            double *S1 = w->seg + ((size_t)t * 3 + 1) * 6 * ld;
+            double *S2 = w->seg + ((size_t)t * 3 + 2) * 6 * ld;
+            double *ss = w->segsums + (size_t)t * 3 * 9 * np;
+            CU(cudaMemcpyAsync(S0, c->st.x, 6 * ld * 8, cudaMemcpyDeviceToDevice, s));
+            int rc = eval_force(c, c->st.x, c->st.v, c->st.m, 1, LD, nullptr, 3, 1, 1, s, false, -1, ss);
+            if (rc) return rc;
+            CU(cudaMemcpyAsync(S1, c->st.xs, 3 * ld * 8, cudaMemcpyDeviceToDevice, s));
+            CU(cudaMemcpyAsync(S1 + 3 * ld, c->st.vs, 3 * ld * 8, cudaMemcpyDeviceToDevice, s));
+            rc = eval_force(c, c->st.xs, c->st.vs, c->st.m, 1, LD, nullptr, 3, 1, 2, s, false, -1, ss + 9 * np);
+            if (rc) return rc;
+            CU(cudaMemcpyAsync(S2, c->st.xs, 3 * ld * 8, cudaMemcpyDeviceToDevice, s));
+            CU(cudaMemcpyAsync(S2 + 3 * ld, c->st.vs, 3 * ld * 8, cudaMemcpyDeviceToDevice, s));
+            rc = eval_force(c, c->st.xs, c->st.vs, c->st.m, 1, LD, nullptr, 3, 1, 3, s, false, -1, ss + 18 * np);
+            if (rc) return rc;
+        }
+        // reverse the segment's steps
+        for (int t = steps - 1; t >= 0; --t) {
+            const double *S0 = w->seg + ((size_t)t * 3 + 0) * 6 * ld;
+            const double *S1 = w->seg + ((size_t)t * 3 + 1) * 6 * ld;
+            const double *S2 = w->seg + ((size_t)t * 3 + 2) * 6 * ld;
+            const double *ss = w->segsums + (size_t)t * 3 * 9 * np;
+            // stage 3 evaluated a2 = F(x2, v2); stage 2 a1 = F(x1, v1); stage 1 a0 = F(x, v)
+            sa.which = 0;
+            k_stage_adj<<<nblk, nthreads, 0, s>>>(sa);
+            int rc = vjp_eval(c, S2, S2 + 3 * ld, ss + 18 * np, ab, xF, vF, w->m0bar + 1, 1, s);
+            if (rc) return rc;
+            sa.which = 1;
+            k_stage_adj<<<nblk, nthreads, 0, s>>>(sa);
+            rc = vjp_eval(c, S1, S1 + 3 * ld, ss + 9 * np, ab, xF, vF, w->m0bar + 1, 1, s);
+            if (rc) return rc;
+            sa.which = 2;
+            k_stage_adj<<<nblk, nthreads, 0, s>>>(sa);
+            rc = vjp_eval(c, S0, S0 + 3 * ld, ss, ab, xF, vF, w->m0bar + 1, 1, s);
+            if (rc) return rc;
+            sa.which = 3;
+            k_stage_adj<<<nblk, nthreads, 0, s>>>(sa);
+            CU(cudaGetLastError());
+        }
+    }
+    CU(cudaMemcpyAsync(hb.data(), Xb, 6 * ld * 8, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(m0bar, w->m0bar + 1, 8, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(c->st.x, final_state.data(), 6 * ld * 8, cudaMemcpyHostToDevice, s));
+    int rc = check_device_err(c);
+    if (rc) return rc;
+    from_soa(hb.data(), xbar_0, c->n, ld);
+    from_soa(hb.data() + 3 * ld, vbar_0, c->n, ld);
+    return PN_OK;
+}

@@ -14,9 +14,10 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
-#include "../../include/pn.h"
-#include "pn_kernels.h"
+#include "pn_ctx.h"
+#include "pn_tune.h"
 
 using namespace pn;
 
@@ -24,7 +25,7 @@ using namespace pn;
 static thread_local int g_last_error = PN_OK;
 static thread_local char g_last_msg[256] = "";
 
-static int set_err(int code, const char *fmt, ...) {
+int pn::set_err(int code, const char *fmt, ...) {
     g_last_error = code;
     if (fmt) {
         va_list ap;
@@ -35,13 +36,6 @@ static int set_err(int code, const char *fmt, ...) {
     return code;
 }
 
-#define CU(call)                                                                             \
-    do {                                                                                     \
-        cudaError_t e_ = (call);                                                             \
-        if (e_ != cudaSuccess)                                                               \
-            return set_err(PN_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),      \
-                           __FILE__, __LINE__);                                              \
-    } while (0)
 
 extern "C" const char *pn_strerror(int s) {
     switch (s) {
@@ -73,43 +67,10 @@ extern "C" int pn_device_count(void) {
 extern "C" const char *pn_version(void) { return "pn-gb300 0.1 (sm_103a)"; }
 
 // ------------------------------------------------------------------ context
-struct pn_ctx {
-    int dev = 0;
-    int nmax = 0, n = 0;
-    int npad = 0;      // padded star capacity (multiple of 256)
-    long long ld = 0;  // state leading dimension
-    pn_params p{};
-    cudaStream_t stream = nullptr;
-    DevState st{};
-    double *state_buf = nullptr;  // backing store of st
-    double *a_aos = nullptr;      // [ld][3] device acceleration (AoS), for pn_force / drop-ins
-    double *in_aos = nullptr;     // [2][ld][3] + [ld] device AoS x, v, m staging (drop-ins)
-    double *spos = nullptr;
-    void *pack = nullptr;
-    TileOrigin *torg = nullptr;
-    double *acc = nullptr;
-    int acc_splits = 0;
-    double *part = nullptr;  // partial sums (prep / finish / energy share one buffer region each)
-    double *glob = nullptr;  // [NGLOB]
-    double *eout = nullptr;  // [4]
-    unsigned *tickets = nullptr;  // [4]
-    int *err = nullptr;
-    double *h_eout = nullptr;     // pinned
-    int *h_err = nullptr;         // pinned
-    double time = 0.0;
-    bool have_state = false;
-    cudaGraphExec_t step_exec = nullptr;
-    bool step_valid = false;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
-    cudaEvent_t evp[6] = {};      // around the three pair launches of a captured step
-    void *flush = nullptr;        // L2 flush buffer (benchmarks only)
-    size_t flush_bytes = 0;
-    pn_stats stats{};
-    PairCfg cfg_force{}, cfg_energy{};
-    bool cfg_set = false;
-};
+// struct pn_ctx: pn_ctx.h
 
-static inline long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
+
+long long pn::round_up(long long a, long long b) { return (a + b - 1) / b * b; }
 
 extern "C" void pn_params_default(pn_params *p) {
     if (!p) return;
@@ -120,31 +81,45 @@ extern "C" void pn_params_default(pn_params *p) {
     p->precision = PN_PREC_FP64;
 }
 
-static bool is_f32(const pn_ctx *c) { return c->p.precision == PN_PREC_MIXED; }
-static int force_mode(const pn_ctx *c) { return c->p.inv_c2 != 0.0 ? MODE_FORCE : MODE_NEWTON; }
+bool pn::is_f32(const pn_ctx *c) { return c->p.precision == PN_PREC_MIXED; }
+int pn::force_mode(const pn_ctx *c) { return c->p.inv_c2 != 0.0 ? MODE_FORCE : MODE_NEWTON; }
 
 // Launch shape of the pair sweep: explicit parameters win; otherwise a heuristic sized for
 // GB300 (152 SMs): enough CTAs for several waves, split along j when there are few i-blocks.
 static PairCfg choose_cfg(const pn_ctx *c, int mode, int nstar) {
     PairCfg k;
     const bool f32 = is_f32(c);
+    // defaults from a shape sweep on GB300 (N = 2k..256k); pn_autotune refines them
     if (f32) {
-        k.ipt = (mode == MODE_NEWTON) ? 4 : 2;
-        k.tj = 128;
+        k.ipt = (mode == MODE_NEWTON || nstar >= 131072) ? 4 : (nstar >= 4096 ? 2 : 1);
+        k.tj = nstar >= 4096 ? 256 : 128;
+        k.js = 1;
     } else {
         k.ipt = 1;
-        k.tj = 64;
+        k.tj = 128;
+        k.js = nstar >= 32768 ? 4 : 2;
     }
-    k.js = 1;
     if (c->p.i_per_thread > 0) k.ipt = c->p.i_per_thread;
     if (c->p.j_split > 0) k.js = c->p.j_split;
     if (c->p.tile_j > 0) k.tj = c->p.tile_j;
     if (!pair_shape_supported(k.ipt, k.js)) { k.ipt = 1; k.js = 1; }
+    const bool explicit_shape = c->p.i_per_thread > 0 || c->p.j_split > 0 || c->p.tile_j > 0 ||
+                                c->p.grid_split > 0;
+    PairCfg tuned;
+    if (!explicit_shape && nstar > 0 && tune_lookup(c->p.precision, mode, nstar, &tuned)) {
+        const int ntiles_t = (nstar + tuned.tj - 1) / tuned.tj;
+        if (tuned.gsplit > ntiles_t) tuned.gsplit = ntiles_t;
+        return tuned;
+    }
     const int bi = pair_block_i(k);
     const int nib = (nstar + bi - 1) / bi;
     const int ntiles = (nstar + k.tj - 1) / k.tj;
-    int g = c->p.grid_split > 0 ? c->p.grid_split : (4 * 152 * 4 + nib - 1) / (nib > 0 ? nib : 1);
-    if (g > 16) g = 16;
+    // j-splits for about 8 waves of 4 CTAs on 152 SMs, keeping >= 4 tiles per split
+    int g = c->p.grid_split > 0 ? c->p.grid_split : (8 * 152 * 4 + nib - 1) / (nib > 0 ? nib : 1);
+    if (c->p.grid_split <= 0) {
+        if (g > 32) g = 32;
+        if (g > ntiles / 4) g = ntiles / 4;
+    }
     if (g > ntiles) g = ntiles;
     if (g < 1) g = 1;
     k.gsplit = g;
@@ -156,7 +131,7 @@ bool pn::pair_shape_supported(int ipt, int js) {
     return ipt == 1 && (js == 2 || js == 4 || js == 8);
 }
 
-static int ensure_acc(pn_ctx *c, int splits) {
+int pn::ensure_acc(pn_ctx *c, int splits) {
     if (splits <= c->acc_splits) return PN_OK;
     if (c->acc) cudaFree(c->acc);
     c->acc = nullptr;
@@ -172,6 +147,7 @@ static int ensure_acc(pn_ctx *c, int splits) {
 
 static void free_ctx(pn_ctx *c) {
     if (!c) return;
+    free_adjoint(c);
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     void *bufs[] = {c->state_buf, c->a_aos, c->in_aos, c->spos, c->pack, c->torg, c->acc,
                     c->part, c->glob, c->eout, c->tickets, c->err};
@@ -269,7 +245,7 @@ extern "C" int pn_set_params(pn_ctx *c, const pn_params *p) {
     return PN_OK;
 }
 
-static void refresh_cfg(pn_ctx *c) {
+void pn::refresh_cfg(pn_ctx *c) {
     if (c->cfg_set) return;
     const int nstar = c->n - 1;
     c->cfg_force = choose_cfg(c, force_mode(c), nstar);
@@ -279,9 +255,9 @@ static void refresh_cfg(pn_ctx *c) {
 
 // One force evaluation.  x, v, m: particle p component k at [p*sp + k*sk] (device).
 // a_out: optional device output (AoS when asp=3, ask=1).  stage: fused integration stage.
-static int eval_force(pn_ctx *c, const double *x, const double *v, const double *m, long long sp,
-                      long long sk, double *a_out, long long asp, long long ask, int stage,
-                      cudaStream_t s, bool timed, int tslot = -1) {
+int pn::eval_force(pn_ctx *c, const double *x, const double *v, const double *m, long long sp,
+                   long long sk, double *a_out, long long asp, long long ask, int stage,
+                   cudaStream_t s, bool timed, int tslot, double *sums_out) {
     const int n = c->n;
     const int nstar = n - 1;
     refresh_cfg(c);
@@ -304,12 +280,13 @@ static int eval_force(pn_ctx *c, const double *x, const double *v, const double 
     qa.nstar = nstar; qa.npad = c->npad; qa.tj = k.tj; qa.ntiles = (nstar + k.tj - 1) / k.tj;
     qa.gsplit = k.gsplit; qa.eps2 = eps2;
     if (timed) CU(cudaEventRecord(c->ev0, s));
-    if (tslot >= 0) CU(cudaEventRecord(c->evp[2 * tslot], s));
+    // external event nodes, so that the events are really recorded when a captured step replays
+    if (tslot >= 0) CU(cudaEventRecordWithFlags(c->evp[2 * tslot], s, cudaEventRecordExternal));
     if (nstar > 0) {
         if (is_f32(c)) CU(launch_pair_f32(mode, k, qa, s));
         else CU(launch_pair_f64(mode, k, qa, s));
     }
-    if (tslot >= 0) CU(cudaEventRecord(c->evp[2 * tslot + 1], s));
+    if (tslot >= 0) CU(cudaEventRecordWithFlags(c->evp[2 * tslot + 1], s, cudaEventRecordExternal));
     if (timed) CU(cudaEventRecord(c->ev1, s));
 
     FinishArgs fa{};
@@ -319,7 +296,7 @@ static int eval_force(pn_ctx *c, const double *x, const double *v, const double 
     fa.pn1 = mode == MODE_FORCE;
     fa.eps = c->p.eps; fa.eps2 = eps2; fa.inv_c2 = c->p.inv_c2; fa.dt = c->p.dt;
     fa.a = a_out; fa.asp = asp; fa.ask = ask;
-    fa.stage = stage; fa.st = c->st; fa.ld = c->ld;
+    fa.stage = stage; fa.st = c->st; fa.ld = c->ld; fa.sums_out = sums_out;
     fa.part = c->part + (size_t)(c->npad / 256 + 2) * 8;
     fa.ticket = &c->tickets[1]; fa.err = c->err;
     CU(launch_finish(fa, s));
@@ -330,7 +307,7 @@ static int eval_force(pn_ctx *c, const double *x, const double *v, const double 
     return PN_OK;
 }
 
-static int check_device_err(pn_ctx *c) {
+int pn::check_device_err(pn_ctx *c) {
     CU(cudaMemcpyAsync(c->h_err, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     int e = *c->h_err;
@@ -478,6 +455,57 @@ extern "C" double pn_time(pn_ctx *c) { return c ? c->time : 0.0; }
 extern "C" int pn_get_stats(pn_ctx *c, pn_stats *s) {
     if (!c || !s) return PN_ERR_INVALID;
     *s = c->stats;
+    return PN_OK;
+}
+
+// ------------------------------------------------------------------ binary checkpoints
+static const char kCkptMagic[8] = {'P', 'N', 'C', 'K', '0', '0', '0', '1'};
+
+extern "C" int pn_save_checkpoint(pn_ctx *c, const char *path, double eouttime, double init_ene) {
+    if (!c || !c->have_state || !path) return set_err(PN_ERR_STATE, "pn_save_checkpoint");
+    const int n = c->n;
+    std::vector<double> x(3 * (size_t)n), v(3 * (size_t)n), m((size_t)n);
+    int rc = pn_get_state(c, x.data(), v.data());
+    if (rc) return rc;
+    CU(cudaMemcpy(m.data(), c->st.m, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+    FILE *f = fopen(path, "wb");
+    if (!f) return set_err(PN_ERR_IO, "cannot open %s", path);
+    const int32_t n32 = n;
+    const double hdr[3] = {c->time, eouttime, init_ene};
+    bool ok = fwrite(kCkptMagic, 1, 8, f) == 8 && fwrite(&n32, 4, 1, f) == 1 && fwrite(hdr, 8, 3, f) == 3 &&
+              fwrite(&c->p, sizeof(pn_params), 1, f) == 1 && fwrite(x.data(), 8, x.size(), f) == x.size() &&
+              fwrite(v.data(), 8, v.size(), f) == v.size() && fwrite(m.data(), 8, m.size(), f) == m.size();
+    ok = (fclose(f) == 0) && ok;
+    return ok ? set_err(PN_OK, nullptr) : set_err(PN_ERR_IO, "write %s", path);
+}
+
+extern "C" int pn_load_checkpoint(pn_ctx *c, const char *path, double *eouttime, double *init_ene) {
+    if (!c || !path) return set_err(PN_ERR_INVALID, "pn_load_checkpoint");
+    FILE *f = fopen(path, "rb");
+    if (!f) return set_err(PN_ERR_IO, "cannot open %s", path);
+    char magic[8];
+    int32_t n32 = 0;
+    double hdr[3];
+    pn_params p{};
+    bool ok = fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kCkptMagic, 8) == 0 && fread(&n32, 4, 1, f) == 1 &&
+              fread(hdr, 8, 3, f) == 3 && fread(&p, sizeof(pn_params), 1, f) == 1;
+    if (!ok || n32 < 1 || n32 > c->nmax) {
+        fclose(f);
+        return set_err(PN_ERR_IO, "%s: not a checkpoint or n out of range", path);
+    }
+    const size_t n = (size_t)n32;
+    std::vector<double> x(3 * n), v(3 * n), m(n);
+    ok = fread(x.data(), 8, x.size(), f) == x.size() && fread(v.data(), 8, v.size(), f) == v.size() &&
+         fread(m.data(), 8, m.size(), f) == m.size();
+    fclose(f);
+    if (!ok) return set_err(PN_ERR_IO, "%s: truncated", path);
+    int rc = pn_set_params(c, &p);
+    if (rc) return rc;
+    rc = pn_set_state(c, n32, x.data(), v.data(), m.data());
+    if (rc) return rc;
+    c->time = hdr[0];
+    if (eouttime) *eouttime = hdr[1];
+    if (init_ene) *init_ene = hdr[2];
     return PN_OK;
 }
 
@@ -653,6 +681,7 @@ extern "C" void energy(double t, double x[][3], double v[][3], double m[], int n
     printf("pot = %22.15e kin = %22.15e \n pot_pn = %22.15e \n  total= %22.15e ratio = %e\n",
            e.pot_n, e.kin_n, e.pot_pn, e.total, e.kin_n / e.pot_n);
     printf(" DE = %e %g\n", DE, t);
+    fflush(stdout);
 }
 
 extern "C" void initial_energy(double x[][3], double v[][3], double m[], int n, double *init_ene,
@@ -663,6 +692,7 @@ extern "C" void initial_energy(double x[][3], double v[][3], double m[], int n, 
     printf("time = %g\n", 0.0);  // :701-703, same format
     printf("pot = %22.15e kin = %22.15e \n pot_pn = %22.15e \n  total= %22.15e ratio = %e\n",
            e.pot_n, e.kin_n, e.pot_pn, e.total, e.kin_n / e.pot_n);
+    fflush(stdout);
     if (init_ene) *init_ene = e.total;  // :705
 }
 
@@ -753,15 +783,22 @@ extern "C" double pn_flops_per_pair(int mode, int precision) {
     }
 }
 
-// Peak FMA throughput probe: each thread runs 8 independent FMA chains (no memory traffic).
+// Peak FMA throughput probe: each thread runs 8 independent FMA chains (no memory traffic),
+// 16 iterations unrolled per loop trip so that loop overhead stays below 1 %.
+template <typename T> __device__ __forceinline__ T probe_fma(T x, T a, T b);
+template <> __device__ __forceinline__ float probe_fma<float>(float x, float a, float b) { return fmaf(x, a, b); }
+template <> __device__ __forceinline__ double probe_fma<double>(double x, double a, double b) { return fma(x, a, b); }
+
 template <typename T>
 static __global__ void k_fma_probe(T *out, int iters, T a, T b) {
     T r[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) r[q] = (T)(threadIdx.x + q);
-    for (int it = 0; it < iters; ++it)
+    for (int it = 0; it < iters; it += 16)
 #pragma unroll
-        for (int q = 0; q < 8; ++q) r[q] = r[q] * a + b;
+        for (int u = 0; u < 16; ++u)
+#pragma unroll
+            for (int q = 0; q < 8; ++q) r[q] = probe_fma<T>(r[q], a, b);
     T s = 0;
 #pragma unroll
     for (int q = 0; q < 8; ++q) s += r[q];
@@ -803,3 +840,68 @@ extern "C" int pn_probe_fma_peak(int precision, double *tflops) {
     *tflops = flops / (best * 1e-3) / 1e12;
     return PN_OK;
 }
+
+// ------------------------------------------------------------------ autotuning
+// Times every candidate launch shape of the force sweep (and, with sweeps & 2, the energy
+// sweep) on the context's current state and keeps the fastest for this precision and size
+// class.  The state is not modified (the sweeps only write work buffers).
+extern "C" int pn_autotune(pn_ctx *c, int sweeps, double *best_ms) {
+    if (!c || !c->have_state) return set_err(PN_ERR_STATE, "pn_autotune: no state");
+    const int nstar = c->n - 1;
+    if (nstar < 1) return PN_OK;
+    int sms = 0;
+    CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->dev));
+    const bool f32 = is_f32(c);
+    const double eps2 = c->p.eps * c->p.eps;
+    const int modes[2] = {force_mode(c), MODE_ENERGY};
+    for (int which = 0; which < 2; ++which) {
+        if (!(sweeps & (1 << which))) continue;
+        const int mode = modes[which];
+        std::vector<PairCfg> cands = tune_candidates(f32, mode, nstar, sms);
+        PairCfg best{};
+        float best_t = 1e30f;
+        for (const PairCfg &k : cands) {
+            int rc = ensure_acc(c, k.gsplit);
+            if (rc) return rc;
+            PrepArgs pa{};
+            pa.x = c->st.x; pa.v = c->st.v; pa.m = c->st.m; pa.sp = 1; pa.sk = c->ld;
+            pa.nstar = nstar; pa.npad = c->npad; pa.nfill = (int)round_up(nstar, 256);
+            pa.tj = k.tj; pa.f32 = f32; pa.eps2 = eps2;
+            pa.pack = c->pack; pa.torg = c->torg; pa.spos = c->spos;
+            pa.part = c->part; pa.glob = c->glob; pa.ticket = &c->tickets[0];
+            CU(launch_prep(pa, c->stream));
+            PairArgs qa{};
+            qa.pack = c->pack; qa.torg = c->torg; qa.spos = c->spos; qa.out = c->acc; qa.err = c->err;
+            qa.nstar = nstar; qa.npad = c->npad; qa.tj = k.tj; qa.ntiles = (nstar + k.tj - 1) / k.tj;
+            qa.gsplit = k.gsplit; qa.eps2 = eps2;
+            float t = 1e30f;
+            for (int rep = 0; rep < 2; ++rep) {  // first launch warms up
+                CU(cudaEventRecord(c->ev0, c->stream));
+                cudaError_t e = f32 ? launch_pair_f32(mode, k, qa, c->stream)
+                                    : launch_pair_f64(mode, k, qa, c->stream);
+                if (e != cudaSuccess) return set_err(PN_ERR_CUDA, "autotune: %s", cudaGetErrorString(e));
+                CU(cudaEventRecord(c->ev1, c->stream));
+                CU(cudaEventSynchronize(c->ev1));
+                float ms = 0.f;
+                CU(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+                if (rep > 0) t = ms;
+            }
+            if (getenv("PN_TUNE_VERBOSE"))
+                fprintf(stderr, "pn_autotune mode %d: ipt %d js %d tj %d gsplit %d: %.3f ms\n", mode, k.ipt,
+                        k.js, k.tj, k.gsplit, t);
+            if (t < best_t) {
+                best_t = t;
+                best = k;
+            }
+        }
+        int rc = check_device_err(c);
+        if (rc) return rc;
+        tune_store(c->p.precision, mode, nstar, best, best_t);
+        if (best_ms) best_ms[which] = best_t;
+    }
+    c->cfg_set = false;
+    c->step_valid = false;
+    return PN_OK;
+}
+
+extern "C" void pn_autotune_clear(void) { tune_clear(); }

@@ -20,6 +20,16 @@ cudaError_t launch_pair_f32(int mode, const PairCfg &c, const PairArgs &a, cudaS
 cudaError_t launch_pair_f64(int mode, const PairCfg &c, const PairArgs &a, cudaStream_t s);
 bool pair_shape_supported(int ipt, int js);
 
+// Persistent ensemble sweep (k_pair_ens): (ipt, js) in {(1,1), (2,1), (1,4)}; tjmax = the
+// largest tile size among the clusters; grid <= 0 = one wave of resident CTAs.
+cudaError_t launch_pair_ens_f32(int mode, int ipt, int js, int tjmax, int grid, const PairArgs *tab,
+                                const int4 *items, int nitems, unsigned *counter, cudaStream_t s);
+cudaError_t launch_pair_ens_f64(int mode, int ipt, int js, int tjmax, int grid, const PairArgs *tab,
+                                const int4 *items, int nitems, unsigned *counter, cudaStream_t s);
+inline bool ens_shape_supported(int ipt, int js) {
+    return (js == 1 && (ipt == 1 || ipt == 2)) || (ipt == 1 && js == 4);
+}
+
 inline int pair_ng(bool f32, int mode) {
     if (f32) return mode == MODE_NEWTON ? ModeInfo<MODE_NEWTON>::NG32
                   : mode == MODE_FORCE  ? ModeInfo<MODE_FORCE>::NG32

@@ -83,13 +83,13 @@ __device__ __forceinline__ void block_sum_dd(DD (&v)[NV], DD *scratch) {
 }
 
 // Last-CTA election after each CTA published its partial.
-__device__ __forceinline__ bool last_block(unsigned *ticket) {
+__device__ __forceinline__ bool last_block(unsigned *ticket, int nblk) {
     __shared__ bool am_last;
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned t = atomicAdd(ticket, 1u);
-        am_last = (t == gridDim.x - 1);
+        am_last = (t == (unsigned)nblk - 1u);
     }
     __syncthreads();
     return am_last;
@@ -99,9 +99,9 @@ __device__ __forceinline__ bool last_block(unsigned *ticket) {
 // Per star j (particle p = j + 1): s = x_p - x_0, q = |s|^2, R = 1/sqrt(q + eps^2) (the
 // reference's rsqrt, Limit-sticky9.c:15-19), and the pack entries; global sums
 // A1 = sum m R, B3 = sum m R^3 s, C = sum m R^3 q, P = sum m v.
-__global__ void __launch_bounds__(256) k_prep(const PrepArgs a) {
+__device__ __forceinline__ void prep_body(const PrepArgs &a, int blk, int nblk) {
     __shared__ double red[32 * NGLOB];
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blk * blockDim.x + threadIdx.x;
     const double eps2 = a.eps2;
     const double x0 = ld_x(a.x, a.sp, a.sk, 0, 0), y0 = ld_x(a.x, a.sp, a.sk, 0, 1),
                  z0 = ld_x(a.x, a.sp, a.sk, 0, 2);
@@ -176,11 +176,11 @@ __global__ void __launch_bounds__(256) k_prep(const PrepArgs a) {
     }
     block_sum<NGLOB>(g, red);
     if (threadIdx.x == 0)
-        for (int q = 0; q < NGLOB; ++q) a.part[(size_t)blockIdx.x * NGLOB + q] = g[q];
-    if (last_block(a.ticket)) {
+        for (int q = 0; q < NGLOB; ++q) a.part[(size_t)blk * NGLOB + q] = g[q];
+    if (last_block(a.ticket, nblk)) {
         double t[NGLOB];
         for (int q = 0; q < NGLOB; ++q) t[q] = 0.0;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+        for (int b = threadIdx.x; b < nblk; b += blockDim.x)
             for (int q = 0; q < NGLOB; ++q) t[q] += __ldcg(&a.part[(size_t)b * NGLOB + q]);
         block_sum<NGLOB>(t, red);
         if (threadIdx.x == 0) {
@@ -223,9 +223,9 @@ __device__ __forceinline__ void stage_update(const FinishArgs &a, int p, const d
     }
 }
 
-__global__ void __launch_bounds__(256) k_finish(const FinishArgs a) {
+__device__ __forceinline__ void finish_body(const FinishArgs &a, int blk, int nblk) {
     __shared__ double red[32 * 3];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blk * blockDim.x + threadIdx.x;
     const double m0 = a.m[0];
     const double eps = a.eps, eps2 = a.eps2, ic2 = a.inv_c2;
     const double *G = a.glob;
@@ -245,6 +245,8 @@ __global__ void __launch_bounds__(256) k_finish(const FinishArgs a) {
             for (int g = 0; g < a.gsplit; ++g) t += a.acc[((size_t)g * a.nacc + k) * a.npad + i];
             S[k] = t;
         }
+        if (a.sums_out)
+            for (int k = 0; k < a.nacc; ++k) a.sums_out[(size_t)k * a.npad + i] = S[k];
         const double Gv[3] = {S[A_GX], S[A_GY], S[A_GZ]};
         double acc3[3];
         for (int k = 0; k < 3; ++k) acc3[k] = Gv[k] - m0 * R3 * s[k];  // Newton incl. BH column
@@ -302,10 +304,10 @@ __global__ void __launch_bounds__(256) k_finish(const FinishArgs a) {
     if (bad) atomicOr(a.err, DEVERR_NONFINITE);
     block_sum<3>(bh, red);
     if (threadIdx.x == 0)
-        for (int k = 0; k < 3; ++k) a.part[(size_t)blockIdx.x * 3 + k] = bh[k];
-    if (last_block(a.ticket)) {
+        for (int k = 0; k < 3; ++k) a.part[(size_t)blk * 3 + k] = bh[k];
+    if (last_block(a.ticket, nblk)) {
         double t[3] = {0.0, 0.0, 0.0};
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+        for (int b = threadIdx.x; b < nblk; b += blockDim.x)
             for (int k = 0; k < 3; ++k) t[k] += __ldcg(&a.part[(size_t)b * 3 + k]);
         block_sum<3>(t, red);
         if (threadIdx.x == 0) {
@@ -327,9 +329,9 @@ __global__ void __launch_bounds__(256) k_finish(const FinishArgs a) {
 // ------------------------------------------------------------------ energy
 // Per star (Limit-sticky9.c:452-556): kinetic, Newtonian potential row, O(N) 1PN term and the
 // pairwise 1PN energy with its self-pair removal; compensated (double-double) sums.
-__global__ void __launch_bounds__(256) k_energy_finish(const EnergyArgs a) {
+__device__ __forceinline__ void energy_body(const EnergyArgs &a, int blk, int nblk) {
     __shared__ DD red[32 * 4];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blk * blockDim.x + threadIdx.x;
     const double m0 = a.m[0], eps = a.eps, eps2 = a.eps2;
     const double v0[3] = {ld_x(a.v, a.sp, a.sk, 0, 0), ld_x(a.v, a.sp, a.sk, 0, 1),
                           ld_x(a.v, a.sp, a.sk, 0, 2)};
@@ -363,12 +365,12 @@ __global__ void __launch_bounds__(256) k_energy_finish(const EnergyArgs a) {
     block_sum_dd<4>(e, red);
     if (threadIdx.x == 0)
         for (int q = 0; q < 4; ++q) {
-            a.part[((size_t)blockIdx.x * 4 + q) * 2] = e[q].hi;
-            a.part[((size_t)blockIdx.x * 4 + q) * 2 + 1] = e[q].lo;
+            a.part[((size_t)blk * 4 + q) * 2] = e[q].hi;
+            a.part[((size_t)blk * 4 + q) * 2 + 1] = e[q].lo;
         }
-    if (last_block(a.ticket)) {
+    if (last_block(a.ticket, nblk)) {
         DD t[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+        for (int b = threadIdx.x; b < nblk; b += blockDim.x)
             for (int q = 0; q < 4; ++q)
                 t[q] = dd_add(t[q], DD{__ldcg(&a.part[((size_t)b * 4 + q) * 2]),
                                        __ldcg(&a.part[((size_t)b * 4 + q) * 2 + 1])});
@@ -388,7 +390,46 @@ __global__ void __launch_bounds__(256) k_energy_finish(const EnergyArgs a) {
     }
 }
 
+// ------------------------------------------------------------------ kernels
+// One system: the block index is the block within the system.
+__global__ void __launch_bounds__(256) k_prep(const PrepArgs a) { prep_body(a, blockIdx.x, gridDim.x); }
+__global__ void __launch_bounds__(256) k_finish(const FinishArgs a) { finish_body(a, blockIdx.x, gridDim.x); }
+__global__ void __launch_bounds__(256) k_energy_finish(const EnergyArgs a) {
+    energy_body(a, blockIdx.x, gridDim.x);
+}
+
+// An ensemble in one launch: blockmap[b] = (cluster, block within the cluster, blocks of the
+// cluster); each cluster's arguments come from a device table.
+__global__ void __launch_bounds__(256) k_prep_ens(const PrepArgs *tab, const int4 *blockmap) {
+    const int4 bm = blockmap[blockIdx.x];
+    const PrepArgs a = tab[bm.x];
+    prep_body(a, bm.y, bm.z);
+}
+__global__ void __launch_bounds__(256) k_finish_ens(const FinishArgs *tab, const int4 *blockmap) {
+    const int4 bm = blockmap[blockIdx.x];
+    const FinishArgs a = tab[bm.x];
+    finish_body(a, bm.y, bm.z);
+}
+__global__ void __launch_bounds__(256) k_energy_ens(const EnergyArgs *tab, const int4 *blockmap) {
+    const int4 bm = blockmap[blockIdx.x];
+    const EnergyArgs a = tab[bm.x];
+    energy_body(a, bm.y, bm.z);
+}
+
 // ------------------------------------------------------------------ launchers
+cudaError_t launch_prep_ens(const PrepArgs *tab, const int4 *blockmap, int nblocks, cudaStream_t s) {
+    k_prep_ens<<<nblocks, 256, 0, s>>>(tab, blockmap);
+    return cudaGetLastError();
+}
+cudaError_t launch_finish_ens(const FinishArgs *tab, const int4 *blockmap, int nblocks, cudaStream_t s) {
+    k_finish_ens<<<nblocks, 256, 0, s>>>(tab, blockmap);
+    return cudaGetLastError();
+}
+cudaError_t launch_energy_ens(const EnergyArgs *tab, const int4 *blockmap, int nblocks, cudaStream_t s) {
+    k_energy_ens<<<nblocks, 256, 0, s>>>(tab, blockmap);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_prep(const PrepArgs &a, cudaStream_t s) {
     const int nb = (a.nfill + 255) / 256;
     k_prep<<<nb, 256, 0, s>>>(a);

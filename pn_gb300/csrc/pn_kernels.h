@@ -42,6 +42,7 @@ struct FinishArgs {
     double *a;            // output acceleration (may be null), [p*asp + k*ask]
     long long asp, ask;
     int stage;            // 0: none; 1..3: fused integration stage update on st
+    double *sums_out;     // optional [nacc][npad]: the per-star pair sums (adjoint reuse)
     DevState st;
     long long ld;
     double *part;
@@ -62,5 +63,10 @@ struct EnergyArgs {
 cudaError_t launch_prep(const PrepArgs &a, cudaStream_t s);
 cudaError_t launch_finish(const FinishArgs &a, cudaStream_t s);
 cudaError_t launch_energy_finish(const EnergyArgs &a, cudaStream_t s);
+// Ensemble forms: one launch over every cluster's blocks (blockmap[b] = cluster, block within
+// the cluster, the cluster's block count, 0), per-cluster arguments from device tables.
+cudaError_t launch_prep_ens(const PrepArgs *tab, const int4 *blockmap, int nblocks, cudaStream_t s);
+cudaError_t launch_finish_ens(const FinishArgs *tab, const int4 *blockmap, int nblocks, cudaStream_t s);
+cudaError_t launch_energy_ens(const EnergyArgs *tab, const int4 *blockmap, int nblocks, cudaStream_t s);
 
 }  // namespace pn

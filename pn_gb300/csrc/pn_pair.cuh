@@ -49,8 +49,20 @@ inline size_t pair_smem_bytes(int ng, int tj, size_t vec_bytes) {
     return 128 + 2 * (size_t)ng * (size_t)tj * vec_bytes;
 }
 
+// Register budget: the FP32 force sweep with 2 i per thread is capped at 128 registers so
+// that 4 CTAs (16 warps) stay resident per SM.
+template <typename T, int MODE, int IPT>
+constexpr int pair_min_blocks() {
+    return (sizeof(T) == 4 && IPT == 2) ? 4 : 1;
+}
+
+// One work item: the i-block starting at ibase against j-range `split` of a.gsplit.  bars/buf
+// are the CTA's two mbarriers and double-buffered tile storage; seq counts the tiles this CTA
+// has consumed before (it selects the stage and the mbarrier phase), so a CTA can run several
+// items back to back.  Returns false when a bounded wait gave up (the CTA must then stop).
 template <typename T, int MODE, int IPT, int JS>
-__global__ void __launch_bounds__(PAIR_NT) k_pair(const PairArgs a) {
+__device__ __forceinline__ bool pair_block(const PairArgs &a, int ibase, int split, uint64_t *bars,
+                                           typename PackVec<T>::V *buf, uint32_t &seq) {
     constexpr int NT = PAIR_NT;
     constexpr bool F32 = sizeof(T) == 4;
     constexpr int NG = F32 ? ModeInfo<MODE>::NG32 : ModeInfo<MODE>::NG64;
@@ -59,15 +71,9 @@ __global__ void __launch_bounds__(PAIR_NT) k_pair(const PairArgs a) {
     using V = typename PackVec<T>::V;
     static_assert(32 % JS == 0, "JS must divide the warp");
 
-    extern __shared__ __align__(128) unsigned char smem[];
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
-    V *buf = reinterpret_cast<V *>(smem + 128);
-
     const int tid = threadIdx.x;
     const int sub = tid % JS;
     const int grp = tid / JS;
-    const int split = blockIdx.y;
-    const int ibase = blockIdx.x * (NI * IPT);
     const int t0 = (int)(((long long)a.ntiles * split) / a.gsplit);
     const int t1 = (int)(((long long)a.ntiles * (split + 1)) / a.gsplit);
     const int tj = a.tj;
@@ -115,13 +121,6 @@ __global__ void __launch_bounds__(PAIR_NT) k_pair(const PairArgs a) {
 #pragma unroll
         for (int q = 0; q < NACC; ++q) run[k][q] = cmp[k][q] = T(0);
 
-    if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-
     const uint32_t gbytes = (uint32_t)tj * (uint32_t)sizeof(V);
     auto issue = [&](int t, int stage) {
         mbar_arrive_expect_tx(&bars[stage], (uint32_t)NG * gbytes);
@@ -130,12 +129,12 @@ __global__ void __launch_bounds__(PAIR_NT) k_pair(const PairArgs a) {
             bulk_g2s(buf + (size_t)(stage * NG + g) * tj, pack + (size_t)g * a.npad + (size_t)t * tj,
                      gbytes, &bars[stage]);
     };
-    if (tid == 0 && t0 < t1) issue(t0, 0);
+    if (tid == 0 && t0 < t1) issue(t0, (int)(seq & 1u));
 
     for (int t = t0; t < t1; ++t) {
-        const int it = t - t0;
-        const int stage = it & 1;
-        const uint32_t phase = (uint32_t)(it >> 1) & 1u;
+        const uint32_t it = seq + (uint32_t)(t - t0);
+        const int stage = (int)(it & 1u);
+        const uint32_t phase = (it >> 1) & 1u;
         const bool next = (t + 1 < t1);
         if (tid == 0 && next) issue(t + 1, stage ^ 1);
         const bool ok = mbar_wait_bounded(&bars[stage], phase);
@@ -144,9 +143,9 @@ __global__ void __launch_bounds__(PAIR_NT) k_pair(const PairArgs a) {
             if (tid == 0) {
                 atomicOr(a.err, DEVERR_TIMEOUT);
                 mbar_wait_bounded(&bars[stage], phase);
-                if (next) mbar_wait_bounded(&bars[stage ^ 1], (uint32_t)((it + 1) >> 1) & 1u);
+                if (next) mbar_wait_bounded(&bars[stage ^ 1], ((it + 1) >> 1) & 1u);
             }
-            return;
+            return false;
         }
         if constexpr (F32) {
             const TileOrigin o = a.torg[t];
@@ -227,6 +226,57 @@ __global__ void __launch_bounds__(PAIR_NT) k_pair(const PairArgs a) {
             if (sub == 0 && i < a.nstar)
                 a.out[((size_t)split * NACC + q) * a.npad + i] = val;
         }
+    }
+    seq += (uint32_t)(t1 - t0 > 0 ? t1 - t0 : 0);
+    return true;
+}
+
+template <typename T, int MODE, int IPT, int JS>
+__global__ void __launch_bounds__(PAIR_NT, (pair_min_blocks<T, MODE, IPT>())) k_pair(const PairArgs a) {
+    using V = typename PackVec<T>::V;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    V *buf = reinterpret_cast<V *>(smem + 128);
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t seq = 0;
+    pair_block<T, MODE, IPT, JS>(a, blockIdx.x * (PAIR_NT / JS * IPT), blockIdx.y, bars, buf, seq);
+}
+
+// Ensemble sweep: one persistent launch over the work items of every cluster.
+// items[w] = (cluster, first i of the block, j-range split, 0), ordered by decreasing cost;
+// tab[cluster] holds that cluster's arguments (pointers offset to its slots, its tile size,
+// split count and softening).  Each CTA takes the next item from *counter until the list is
+// exhausted: the counter only grows, so every CTA leaves after at most nitems + 1 fetches.
+// The counter is zeroed before each launch.
+template <typename T, int MODE, int IPT, int JS>
+__global__ void __launch_bounds__(PAIR_NT, (pair_min_blocks<T, MODE, IPT>()))
+    k_pair_ens(const PairArgs *tab, const int4 *items, int nitems, unsigned *counter) {
+    using V = typename PackVec<T>::V;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    V *buf = reinterpret_cast<V *>(smem + 128);
+    __shared__ int cur;
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t seq = 0;
+    for (;;) {
+        if (threadIdx.x == 0) cur = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int w = cur;
+        __syncthreads();  // everyone has read cur before thread 0 fetches the next item
+        if (w >= nitems) break;
+        const int4 it = items[w];
+        const PairArgs a = tab[it.x];
+        if (!pair_block<T, MODE, IPT, JS>(a, it.y, it.z, bars, buf, seq)) break;
     }
 }
 

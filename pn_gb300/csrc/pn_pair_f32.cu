@@ -46,3 +46,54 @@ cudaError_t launch_pair_f32(int mode, const PairCfg &c, const PairArgs &a, cudaS
 }
 
 }  // namespace pn
+
+namespace pn {
+
+template <int MODE, int IPT, int JS>
+static cudaError_t launch_ens_one(int tjmax, int grid, const PairArgs *tab, const int4 *items,
+                                  int nitems, unsigned *counter, cudaStream_t s) {
+    constexpr bool F32 = sizeof(float) == 4;
+    const int ng = F32 ? ModeInfo<MODE>::NG32 : ModeInfo<MODE>::NG64;
+    const size_t smem = pair_smem_bytes(ng, tjmax, sizeof(float4));
+    auto fn = k_pair_ens<float, MODE, IPT, JS>;
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    if (grid <= 0) {  // persistent: as many CTAs as fit on the GPU at once
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, PAIR_NT, smem);
+        grid = sms * (per > 0 ? per : 1);
+    }
+    fn<<<grid, PAIR_NT, smem, s>>>(tab, items, nitems, counter);
+    return cudaGetLastError();
+}
+
+template <int MODE>
+static cudaError_t launch_ens_mode(int ipt, int js, int tjmax, int grid, const PairArgs *tab,
+                                   const int4 *items, int nitems, unsigned *counter, cudaStream_t s) {
+    if (js == 1) {
+        if (ipt == 1) return launch_ens_one<MODE, 1, 1>(tjmax, grid, tab, items, nitems, counter, s);
+        if (ipt == 2) return launch_ens_one<MODE, 2, 1>(tjmax, grid, tab, items, nitems, counter, s);
+    } else if (ipt == 1 && js == 4) {
+        return launch_ens_one<MODE, 1, 4>(tjmax, grid, tab, items, nitems, counter, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_pair_ens_f32(int mode, int ipt, int js, int tjmax, int grid, const PairArgs *tab,
+                                 const int4 *items, int nitems, unsigned *counter, cudaStream_t s) {
+    if (nitems <= 0) return cudaSuccess;
+    switch (mode) {
+        case MODE_NEWTON: return launch_ens_mode<MODE_NEWTON>(ipt, js, tjmax, grid, tab, items, nitems, counter, s);
+        case MODE_FORCE: return launch_ens_mode<MODE_FORCE>(ipt, js, tjmax, grid, tab, items, nitems, counter, s);
+        case MODE_ENERGY: return launch_ens_mode<MODE_ENERGY>(ipt, js, tjmax, grid, tab, items, nitems, counter, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace pn

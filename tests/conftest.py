@@ -51,3 +51,24 @@ def relerr(a, b):
     """Per-particle normwise relative error |a_i - b_i| / |b_i|."""
     import numpy as np
     return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+
+
+def assert_matches_reference(a, a_ref, a_exact, tol=1e-12):
+    """FP64 parity with the reference, particle by particle.
+
+    Every particle must be within tol (normwise relative) of the exact value of the
+    reference's formulas (a_exact: the same algorithm in long double).  Against the reference
+    itself every particle must be within tol too, except where the reference's own double
+    rounding is larger than tol (|a_ref - a_exact| > tol |a_exact|); there the difference must
+    stay within that rounding error plus tol."""
+    import numpy as np
+    e_exact = relerr(a, a_exact)
+    assert e_exact.max() <= tol, ("vs exact", int(e_exact.argmax()), float(e_exact.max()))
+    e_ref = relerr(a, a_ref)
+    own = relerr(a_ref, a_exact)
+    bad = e_ref > tol
+    assert (own[bad] > tol).all(), ("vs reference where it is accurate",
+                                    np.nonzero(bad & (own <= tol))[0][:5])
+    na = np.linalg.norm(a_exact, axis=1)
+    lim = np.linalg.norm(a_ref - a_exact, axis=1) + tol * na
+    assert (np.linalg.norm(a - a_ref, axis=1) <= lim).all()

@@ -8,6 +8,11 @@ exists; the .npz files it writes are committed, so the tests do not need the ref
 
     python tests/golden/make_golden.py [case ...]      (cases: kat random init10k config1)
 
+Every case also stores a_exact: force() of the same input evaluated by the oracle's
+long-double build (the reference's formulas with a 64-bit significand).  Where the reference's
+own double rounding exceeds the test tolerance -- the BH of a symmetric cluster, whose net
+acceleration is orders of magnitude below the sum of its terms -- the tests measure against it.
+
 Cases
   kat      hand-placed BH + 1..3 stars with velocities (n = 2, 3, 4): force, energy, 1 step
   random   n = 1001, positions uniform in [-1,1]^3, velocities N(0, 0.3^2), random masses:
@@ -56,6 +61,7 @@ def case_kat():
     for k, (x, v, m) in cases.items():
         out[k + "_x"], out[k + "_v"], out[k + "_m"] = x, v, m
         out[k + "_a"] = po.ref_force(x, v, m, eps)
+        out[k + "_a_exact"] = po.force_exact(x, v, m, eps)
         out[k + "_e"] = np.array([po.ref_initial_energy(x, v, m, eps)])
         x1, v1 = po.ref_run(x, v, m, eps, dt, 1)
         out[k + "_x1"], out[k + "_v1"] = x1, v1
@@ -75,8 +81,8 @@ def case_random():
     a = po.ref_force(x, v, m, eps)
     e = po.ref_initial_energy(x, v, m, eps)
     x5, v5 = po.ref_run(x, v, m, eps, dt, 5)
-    _save("random_1001.npz", x=x, v=v, m=m, a=a, e=np.array([e]), x5=x5, v5=v5,
-          eps=np.array([eps]), dt=np.array([dt]))
+    _save("random_1001.npz", x=x, v=v, m=m, a=a, a_exact=po.force_exact(x, v, m, eps),
+          e=np.array([e]), x5=x5, v5=v5, eps=np.array([eps]), dt=np.array([dt]))
 
 
 def case_init10k():
@@ -97,8 +103,8 @@ def case_init10k():
     a = po.ref_force(x, v, m, eps)
     e = po.ref_initial_energy(x, v, m, eps)
     x10, v10 = po.ref_run(x, v, m, eps, dt, 10)
-    _save("init10k_2000.npz", xs=xs.astype(np.float32), a=a, e=np.array([e]), x10=x10, v10=v10,
-          eps=np.array([eps]), dt=np.array([dt]))
+    _save("init10k_2000.npz", xs=xs.astype(np.float32), a=a, a_exact=po.force_exact(x, v, m, eps),
+          e=np.array([e]), x10=x10, v10=v10, eps=np.array([eps]), dt=np.array([dt]))
 
 
 def case_config1(nsteps=100):
@@ -112,9 +118,21 @@ def case_config1(nsteps=100):
     xT, vT = po.ref_run(s.x, s.v, s.m, eps, dt, nsteps)
     print("config1 run", time.time() - t0, "s", flush=True)
     eT = po.ref_initial_energy(xT, vT, s.m, eps)
-    _save("config1.npz", xs=s.x[1:].astype(np.float32), m=s.m, a=a, e0=np.array([e0]),
+    _save("config1.npz", xs=s.x[1:].astype(np.float32), m=s.m, a=a,
+          a_exact=po.force_exact(s.x, s.v, s.m, eps), e0=np.array([e0]),
           xT=xT, vT=vT, eT=np.array([eT]), nsteps=np.array([nsteps]), eps=np.array([eps]),
           dt=np.array([dt]))
+
+
+def case_config1_exact():
+    """Adds the long-double force to an existing config1.npz."""
+    path = os.path.join(HERE, "config1.npz")
+    g = dict(np.load(path))
+    n = g["xs"].shape[0] + 1
+    x = np.zeros((n, 3))
+    x[1:] = g["xs"].astype(np.float64)
+    g["a_exact"] = po.force_exact(x, np.zeros((n, 3)), g["m"], float(g["eps"][0]))
+    _save("config1.npz", **g)
 
 
 if __name__ == "__main__":
@@ -123,4 +141,5 @@ if __name__ == "__main__":
         sys.exit("the reference source is not present; golden vectors cannot be regenerated here")
     which = sys.argv[1:] or ["kat", "random", "init10k", "config1"]
     for w in which:
-        {"kat": case_kat, "random": case_random, "init10k": case_init10k, "config1": case_config1}[w]()
+        {"kat": case_kat, "random": case_random, "init10k": case_init10k, "config1": case_config1,
+         "config1_exact": case_config1_exact}[w]()

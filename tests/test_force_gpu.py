@@ -3,6 +3,9 @@
 Tolerances (FP64 mode, per particle, normwise |a_i - a_ref,i| / |a_ref,i|):
   accelerations <= 1e-12, energies <= 1e-12 (relative), trajectories <= 1e-10 (relative to the
   largest coordinate), as the summation order differs from the reference's sequential loops.
+  Where the reference's own double rounding exceeds 1e-12 (the BH of a symmetric cluster,
+  whose net acceleration is far below the sum of its terms), accelerations are checked against
+  the long-double evaluation of the reference's formulas (conftest.assert_matches_reference).
 Mixed mode (FP32 pair terms) is checked against the FP64 GPU path and the oracle with the
 error bounds stated at each test.
 """
@@ -11,7 +14,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from conftest import golden, relerr
+from conftest import assert_matches_reference, golden, relerr
 
 pytestmark = pytest.mark.gpu
 
@@ -49,7 +52,7 @@ def test_kat_small(pn):
         x, v, m = g[k + "_x"], g[k + "_v"], g[k + "_m"]
         with pn.Context(x.shape[0], eps=eps, dt=dt) as c:
             c.set_state(x, v, m)
-            assert relerr(c.force(), g[k + "_a"]).max() <= TOL_A, k
+            assert_matches_reference(c.force(), g[k + "_a"], g[k + "_a_exact"], TOL_A)
             assert abs(c.energy()[3] / g[k + "_e"][0] - 1) <= TOL_E, k
             c.steps(1)
             x1, v1 = c.get_state()
@@ -61,7 +64,7 @@ def test_random_1001(pn):
     eps, dt = float(g["eps"][0]), float(g["dt"][0])
     with pn.Context(1001, eps=eps, dt=dt) as c:
         c.set_state(g["x"], g["v"], g["m"])
-        assert relerr(c.force(), g["a"]).max() <= TOL_A
+        assert_matches_reference(c.force(), g["a"], g["a_exact"], TOL_A)
         assert abs(c.energy()[3] / g["e"][0] - 1) <= TOL_E
         c.steps(5)
         x5, v5 = c.get_state()
@@ -82,7 +85,7 @@ def test_init10k_reference_file(pn):
     eps, dt = float(g["eps"][0]), float(g["dt"][0])
     with pn.Context(n, eps=eps, dt=dt) as c:
         c.set_state(x, v, m)
-        assert relerr(c.force(), g["a"]).max() <= TOL_A
+        assert_matches_reference(c.force(), g["a"], g["a_exact"], TOL_A)
         assert abs(c.energy()[3] / g["e"][0] - 1) <= TOL_E
         c.steps(10)
         x10, v10 = c.get_state()
@@ -102,7 +105,7 @@ def test_config1_uniform_sphere_100_steps(pn):
     assert np.array_equal(s.x, x)
     with pn.Context(n, eps=eps, dt=dt) as c:
         c.set_state(x, v, g["m"])
-        assert relerr(c.force(), g["a"]).max() <= TOL_A
+        assert_matches_reference(c.force(), g["a"], g["a_exact"], TOL_A)
         assert abs(c.energy()[3] / g["e0"][0] - 1) <= TOL_E
         c.steps(int(g["nsteps"][0]))
         xT, vT = c.get_state()
@@ -121,7 +124,7 @@ SHAPES = [dict(), dict(i_per_thread=1), dict(i_per_thread=4), dict(j_split=2), d
 def test_fp64_ragged_sizes(pn, oracle, n):
     x, v, m = random_system(n, n)
     a = ctx_force(pn, x, v, m, 0.02)
-    assert relerr(a, oracle.force(x, v, m, 0.02)).max() <= TOL_A
+    assert relerr(a, oracle.force_exact(x, v, m, 0.02)).max() <= TOL_A
 
 
 @pytest.mark.parametrize("shape", SHAPES, ids=[str(s) for s in SHAPES])
@@ -129,11 +132,16 @@ def test_fp64_ragged_sizes(pn, oracle, n):
 def test_launch_shapes(pn, oracle, shape, prec):
     x, v, m = random_system(777, 5)
     a = ctx_force(pn, x, v, m, 0.02, precision=prec, **shape)
-    e = relerr(a, oracle.force(x, v, m, 0.02))
+    ax = oracle.force_exact(x, v, m, 0.02)
+    e = relerr(a, ax)
     if prec == 0:
         assert e.max() <= TOL_A
     else:
-        assert np.sqrt((e ** 2).mean()) <= 2e-6 and e.max() <= 1e-4
+        # c = 1 on a uniform random cube: Newtonian and 1PN terms cancel on many particles, so
+        # the error is bounded against the RMS acceleration (per-particle: loose)
+        d = np.linalg.norm(a - ax, axis=1)
+        assert np.sqrt((d ** 2).mean() / (np.linalg.norm(ax, axis=1) ** 2).mean()) <= 1e-6
+        assert e.max() <= 1e-3
 
 
 def test_energy_with_moving_bh(pn, oracle):
@@ -186,7 +194,7 @@ def test_newtonian_only(pn, oracle):
     an = oracle.force_newton(x, m, 0.02)
     assert relerr(ctx_force(pn, x, v, m, 0.02, inv_c2=0.0), an).max() <= TOL_A
     e = relerr(ctx_force(pn, x, v, m, 0.02, inv_c2=0.0, precision=1), an)
-    assert np.sqrt((e ** 2).mean()) <= 2e-6
+    assert np.sqrt((e ** 2).mean()) <= 1e-6
 
 
 @pytest.mark.parametrize("cval", [10.0, 1000.0])
@@ -245,7 +253,7 @@ def test_dropin_force_and_energy_output(pn, oracle, capfd):
     assert out[0] == "time = 0"
     assert out[1].startswith("pot = ") and " kin = " in out[1]
     assert out[2].startswith(" pot_pn = ") and out[3].startswith("  total= ")
-    assert out[5] == "time = 0.5" and out[-1].startswith(" DE = ") and out[-1].endswith(" 0.5")
+    assert out[4] == "time = 0.5" and out[-1].startswith(" DE = ") and out[-1].endswith(" 0.5")
     de = float(out[-1].split()[2])
     assert abs(de) < 1e-12
 
@@ -254,10 +262,12 @@ def test_dropin_mixed_precision(pn, oracle):
     x, v, m = random_system(2000, 22)
     pn.configure(pn.PN_PREC_MIXED, 1.0)
     try:
-        e = relerr(pn.force(x, v, m, 0.02), oracle.force(x, v, m, 0.02))
+        a = pn.force(x, v, m, 0.02)
     finally:
         pn.configure(pn.PN_PREC_FP64, 1.0)
-    assert np.sqrt((e ** 2).mean()) <= 2e-6
+    ax = oracle.force_exact(x, v, m, 0.02)
+    d = np.linalg.norm(a - ax, axis=1)
+    assert np.sqrt((d ** 2).mean() / (np.linalg.norm(ax, axis=1) ** 2).mean()) <= 1e-6
 
 
 def test_force_device_pointers(pn, oracle):
