@@ -203,6 +203,141 @@ def run_reference(args, rank, world, dist):
     return 0
 
 
+def run_ensemble(args):
+    """Configuration 4: 256 Plummer + BH clusters, N log-uniform in [1024, 65536], BH mass
+    fraction log-uniform in [1e-3, 1e-1], eps = 0.01, dt = 1/1024, mixed precision, one
+    persistent pair launch per force evaluation, each step one CUDA graph.  Times K steps
+    (interactions/s = sum n_c^2 per evaluation, 3 per step) and checks a subset of clusters
+    against individual FP64 runs."""
+    import pn_gb300 as pn
+    rng = np.random.default_rng(4)
+    nc = args.clusters
+    sizes = np.exp(rng.uniform(np.log(1024), np.log(65536), nc)).astype(int)
+    fracs = np.exp(rng.uniform(np.log(1e-3), np.log(1e-1), nc))
+    systems = [pn.config_plummer(int(s), 1000 + k, float(f)) for k, (s, f) in enumerate(zip(sizes, fracs))]
+    eps = [0.01] * nc
+    inter = 3.0 * sum(float(s.x.shape[0]) ** 2 for s in systems)
+    e = pn.Ensemble(systems, eps, dt=DT, inv_c2=INV_C2, precision=pn.PN_PREC_MIXED)
+    t0 = time.perf_counter()
+    e.autotune()
+    tune_s = time.perf_counter() - t0
+    e.bench_steps(args.warmup)
+    with ClockSampler() as clk:
+        ms = e.bench_steps(args.steps)
+    total = float(ms.sum())
+    # cluster-by-cluster check: the ensemble (mixed) after the warm-up and timed steps against
+    # individual FP64 contexts run for the same number of steps
+    nsteps = args.warmup + args.steps
+    xs, vs = e.get_state()
+    e.close()
+    picks = sorted(set([int(np.argmin(sizes)), int(np.argmax(sizes))] + list(rng.choice(nc, 4, replace=False))))
+    errs = {}
+    for k in picks:
+        s = systems[k]
+        with pn.Context(s.x.shape[0], eps=eps[k], dt=DT, inv_c2=INV_C2) as c:
+            c.set_state(s.x, s.v, s.m)
+            c.steps(nsteps)
+            xr, vr = c.get_state()
+        errs[str(k)] = {"n": int(s.x.shape[0]),
+                        "max_pos_err_rel": float(np.abs(xs[k] - xr).max() / np.abs(xr).max()),
+                        "max_vel_err_rel": float(np.abs(vs[k] - vr).max() / np.abs(vr).max())}
+    line = {"metric": "interactions/s, ensemble of 256 clusters (persistent launch, CUDA graph steps)",
+            "value": args.steps * inter / (total * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": f"ensemble_{nc}_plummer_bh", "n_range": [int(sizes.min()), int(sizes.max())],
+                       "particles": int(sum(s.x.shape[0] for s in systems)), "eps": 0.01, "dt": DT,
+                       "inv_c2": INV_C2, "autotune_s": tune_s},
+            "clocks": clk.summary(), "check_vs_individual_fp64": errs}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_adjoint(args):
+    """Configuration 5: N = 16384 Plummer + BH (mass fraction 0.05), 200 steps at dt = 1/1024,
+    checkpoints every 20 steps.  Loss: squared distance of the final snapshot (x, v) to a
+    target made with the BH mass x 1.1 and initial positions + N(0, 1e-3^2).  Reports the
+    adjoint's cost per step against a forward step, and checks the FP64 gradient against
+    central finite differences (h = 1e-6) on sampled coordinates and the BH mass, and the
+    mixed-precision gradient against the FP64 one."""
+    import pn_gb300 as pn
+    ns, nsteps, K = args.adj_n, args.adj_steps, 20
+    s = pn.config_plummer(ns, 77, 0.05)
+    eps = pn.plummer_eps(ns)
+    rng = np.random.default_rng(5)
+    n = ns + 1
+
+    def final(x, v, m, prec=0, steps=nsteps):
+        with pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=prec) as c:
+            c.set_state(x, v, m)
+            c.steps(steps)
+            return c.get_state()
+
+    mt = s.m.copy()
+    mt[0] *= 1.1
+    xt0 = s.x + rng.normal(0, 1e-3, s.x.shape)
+    xt0[0] = s.x[0]
+    xT, vT = final(xt0, s.v, mt)
+
+    def loss(x, v, m):
+        xe, ve = final(x, v, m)
+        return float(((xe - xT) ** 2).sum() + ((ve - vT) ** 2).sum())
+
+    out = {}
+    for prec in (0, 1):
+        with pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=prec) as c:
+            c.set_state(s.x, s.v, s.m)
+            c.steps(2)  # warm-up (graph, kernels)
+            c.sync()
+            c.set_state(s.x, s.v, s.m)
+            t0 = time.perf_counter()
+            c.steps(nsteps)
+            c.sync()
+            fwd = (time.perf_counter() - t0) / nsteps
+            c.set_state(s.x, s.v, s.m)
+            c.adjoint_forward(nsteps, K)
+            xe, ve = c.get_state()
+            t0 = time.perf_counter()
+            gx, gv, gm = c.adjoint_backward(2 * (xe - xT), 2 * (ve - vT))
+            bwd = (time.perf_counter() - t0) / nsteps
+        out[prec] = dict(fwd_ms=fwd * 1e3, adj_ms=bwd * 1e3, gx=gx, gv=gv, gm=gm)
+    # central differences on sampled coordinates (FP64 forward runs)
+    h = 1e-6
+    checks = []
+    for q in rng.choice(np.arange(3, 3 * n), args.fd_coords, replace=False):
+        p, k = divmod(int(q), 3)
+        for which in ("x", "v"):
+            a = (s.x if which == "x" else s.v).copy()
+            b = a.copy()
+            a[p, k] += h
+            b[p, k] -= h
+            lp = loss(a, s.v, s.m) if which == "x" else loss(s.x, a, s.m)
+            lm = loss(b, s.v, s.m) if which == "x" else loss(s.x, b, s.m)
+            fd = (lp - lm) / (2 * h)
+            g = out[0]["gx" if which == "x" else "gv"][p, k]
+            checks.append(abs(g - fd) / max(abs(fd), 1e-12))
+    mp, mm = s.m.copy(), s.m.copy()
+    mp[0] += h
+    mm[0] -= h
+    fdm = (loss(s.x, s.v, mp) - loss(s.x, s.v, mm)) / (2 * h)
+    rel_m = abs(out[0]["gm"] - fdm) / abs(fdm)
+    dmix = np.linalg.norm(out[1]["gx"] - out[0]["gx"]) / np.linalg.norm(out[0]["gx"])
+    line = {"metric": "adjoint cost per step / forward step (N=16384, 200 steps, checkpoints every 20)",
+            "value": out[1]["adj_ms"] / out[1]["fwd_ms"], "unit": "ratio", "n_gpus": 1, "steps": nsteps,
+            "warmup": 2, "higher_is_better": False, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": f"plummer_bh_N{ns}_adjoint", "bh_mass_fraction": 0.05, "dt": DT,
+                       "checkpoint_every": K, "inv_c2": INV_C2},
+            "mixed": {"fwd_ms_per_step": out[1]["fwd_ms"], "adj_ms_per_step": out[1]["adj_ms"]},
+            "fp64": {"fwd_ms_per_step": out[0]["fwd_ms"], "adj_ms_per_step": out[0]["adj_ms"],
+                     "ratio": out[0]["adj_ms"] / out[0]["fwd_ms"]},
+            "fd_check_fp64": {"coords": len(checks), "max_rel_err": float(max(checks)),
+                              "median_rel_err": float(np.median(checks)), "bh_mass_rel_err": float(rel_m)},
+            "mixed_vs_fp64_grad_rel": float(dmix),
+            "mixed_vs_fp64_dm0_rel": float(abs(out[1]["gm"] / out[0]["gm"] - 1))}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def profile_case(nstars):
     """One mixed-precision force evaluation of the bench workload at nstars (ncu target)."""
     import pn_gb300 as pn
@@ -246,9 +381,19 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the FP64, accuracy and CPU legs")
     ap.add_argument("--profile-case", type=int, default=0, metavar="N",
                     help="set up N stars, tune, run one mixed force evaluation and exit (for ncu)")
+    ap.add_argument("--ensemble", action="store_true", help="configuration 4 (ensemble) instead")
+    ap.add_argument("--clusters", type=int, default=256)
+    ap.add_argument("--adjoint", action="store_true", help="configuration 5 (adjoint) instead")
+    ap.add_argument("--adj-n", type=int, default=16384)
+    ap.add_argument("--adj-steps", type=int, default=200)
+    ap.add_argument("--fd-coords", type=int, default=2)
     args = ap.parse_args()
     if args.profile_case:
         return profile_case(args.profile_case)
+    if args.ensemble:
+        return run_ensemble(args)
+    if args.adjoint:
+        return run_adjoint(args)
     rank, world, dist = dist_init(args.gpus)
     if args.impl == "reference":
         return run_reference(args, rank, world, dist)

@@ -64,7 +64,14 @@ typedef struct {
     int i_per_thread;  /* i-particles held per thread; 0 = tuned */
     int j_split;       /* lanes sharing one i-set (warp-shuffle reduction); 0 = tuned */
     int grid_split;    /* CTAs sharing one i-block (partial sums reduced in FP64); 0 = tuned */
+    int pair_variant;  /* mixed mode: PN_PAIR_AUTO (0, tuned), PN_PAIR_SCALAR (1) or
+                          PN_PAIR_F32X2 (2: packed FP32x2 instructions, two j per instruction) */
+    int integrator;    /* PN_INT_REFERENCE (0): the reference's 3-evaluation scheme
+                          (Limit-sticky9.c:844-893); PN_INT_RK4 (1): classic 4th-order RK */
 } pn_params;
+
+enum { PN_PAIR_AUTO = 0, PN_PAIR_SCALAR = 1, PN_PAIR_F32X2 = 2 };
+enum { PN_INT_REFERENCE = 0, PN_INT_RK4 = 1 };
 
 /* Energies as the reference prints them (Limit-sticky9.c:561-562, :702-703). */
 typedef struct {

@@ -45,7 +45,8 @@ class Params(ctypes.Structure):
     _fields_ = [("eps", ctypes.c_double), ("dt", ctypes.c_double), ("inv_c2", ctypes.c_double),
                 ("precision", ctypes.c_int), ("tile_j", ctypes.c_int),
                 ("i_per_thread", ctypes.c_int), ("j_split", ctypes.c_int),
-                ("grid_split", ctypes.c_int)]
+                ("grid_split", ctypes.c_int), ("pair_variant", ctypes.c_int),
+                ("integrator", ctypes.c_int)]
 
 
 class Energy(ctypes.Structure):
@@ -90,6 +91,8 @@ SIGNATURES = [
     ("pn_time", ctypes.c_double, [ctypes.c_void_p]),
     ("pn_get_stats", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
     ("pn_set_params", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Params)]),
+    ("pn_save_checkpoint", ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_double, ctypes.c_double]),
+    ("pn_load_checkpoint", ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, _dp, _dp]),
     ("pn_force_device", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p]),

@@ -105,12 +105,30 @@ static PairCfg choose_cfg(const pn_ctx *c, int mode, int nstar) {
     if (!pair_shape_supported(k.ipt, k.js)) { k.ipt = 1; k.js = 1; }
     const bool explicit_shape = c->p.i_per_thread > 0 || c->p.j_split > 0 || c->p.tile_j > 0 ||
                                 c->p.grid_split > 0;
+    // the packed f32x2 sweep: JS = 1 and 1 or 2 i per thread; explicit choice or tuned
+    const bool x2_ok = f32 && k.js == 1 && k.ipt <= 2;
+    const int pv = c->p.pair_variant;
     PairCfg tuned;
-    if (!explicit_shape && nstar > 0 && tune_lookup(c->p.precision, mode, nstar, &tuned)) {
+    if (!explicit_shape && pv == PN_PAIR_AUTO && nstar > 0 &&
+        tune_lookup(c->p.precision, mode, nstar, &tuned)) {
         const int ntiles_t = (nstar + tuned.tj - 1) / tuned.tj;
         if (tuned.gsplit > ntiles_t) tuned.gsplit = ntiles_t;
         return tuned;
     }
+    if (pv == PN_PAIR_F32X2 && f32) {
+        if (k.ipt > 2) k.ipt = 2;
+        if (k.js != 1) k.js = 1;
+        k.x2 = 1;
+    } else if (pv == PN_PAIR_AUTO && f32 && !explicit_shape) {
+        // untuned default of the mixed sweep: the packed f32x2 form, 2 i per thread for
+        // N >= 4096 (fastest in the tuner's measurements at N = 2^18: 111 ms vs 125 ms)
+        k.ipt = nstar >= 4096 ? 2 : 1;
+        k.js = 1;
+        k.x2 = 1;
+    } else {
+        k.x2 = 0;  // scalar sweep: FP64, PN_PAIR_SCALAR, or an explicit shape without the variant
+    }
+    (void)x2_ok;
     const int bi = pair_block_i(k);
     const int nib = (nstar + bi - 1) / bi;
     const int ntiles = (nstar + k.tj - 1) / k.tj;
@@ -149,7 +167,7 @@ static void free_ctx(pn_ctx *c) {
     if (!c) return;
     free_adjoint(c);
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
-    void *bufs[] = {c->state_buf, c->a_aos, c->in_aos, c->spos, c->pack, c->torg, c->acc,
+    void *bufs[] = {c->state_buf, c->a_aos, c->in_aos, c->spos, c->pack, c->pack2, c->ipack, c->torg, c->acc,
                     c->part, c->glob, c->eout, c->tickets, c->err};
     for (void *b : bufs)
         if (b) cudaFree(b);
@@ -173,6 +191,8 @@ static int validate_params(const pn_params *p) {
         return PN_ERR_INVALID;
     if (p->i_per_thread < 0 || p->j_split < 0 || p->grid_split < 0 || p->grid_split > 64)
         return PN_ERR_INVALID;
+    if (p->pair_variant < PN_PAIR_AUTO || p->pair_variant > PN_PAIR_F32X2) return PN_ERR_INVALID;
+    if (p->integrator != PN_INT_REFERENCE && p->integrator != PN_INT_RK4) return PN_ERR_INVALID;
     if ((p->i_per_thread || p->j_split) &&
         !pair_shape_supported(p->i_per_thread ? p->i_per_thread : 1, p->j_split ? p->j_split : 1))
         return PN_ERR_INVALID;
@@ -207,6 +227,9 @@ extern "C" int pn_create(pn_ctx **out, int nmax, const pn_params *p) {
     if (cudaMalloc(&c->in_aos, 7 * ld * sizeof(double)) != cudaSuccess) return fail("in");
     if (cudaMalloc(&c->spos, 3 * np * sizeof(double)) != cudaSuccess) return fail("spos");
     if (cudaMalloc(&c->pack, 6 * np * 16) != cudaSuccess) return fail("pack");
+    if (cudaMalloc(&c->pack2, 7 * (np / 2) * 16) != cudaSuccess) return fail("pack2");
+    if (cudaMalloc(&c->ipack, np * 16) != cudaSuccess) return fail("ipack");
+    if (cudaMemset(c->pack2, 0, 7 * (np / 2) * 16) != cudaSuccess) return fail("memset");
     if (cudaMalloc(&c->torg, (np / 32 + 1) * sizeof(TileOrigin)) != cudaSuccess) return fail("torg");
     const size_t nblk = np / 256 + 2;
     if (cudaMalloc(&c->part, nblk * 8 * 2 * sizeof(double)) != cudaSuccess) return fail("part");
@@ -272,11 +295,12 @@ int pn::eval_force(pn_ctx *c, const double *x, const double *v, const double *m,
     pa.nstar = nstar; pa.npad = c->npad; pa.nfill = (int)round_up(nstar > 0 ? nstar : 1, 256);
     pa.tj = k.tj; pa.f32 = is_f32(c); pa.eps2 = eps2;
     pa.pack = c->pack; pa.torg = c->torg; pa.spos = c->spos;
+    if (pa.f32) { pa.pack2 = c->pack2; pa.ipack = c->ipack; }
     pa.part = c->part; pa.glob = c->glob; pa.ticket = &c->tickets[0];
     CU(launch_prep(pa, s));
 
     PairArgs qa{};
-    qa.pack = c->pack; qa.torg = c->torg; qa.spos = c->spos; qa.out = c->acc; qa.err = c->err;
+    qa.pack = c->pack; qa.torg = c->torg; qa.spos = c->spos; qa.pack2 = c->pack2; qa.ipack = c->ipack; qa.out = c->acc; qa.err = c->err;
     qa.nstar = nstar; qa.npad = c->npad; qa.tj = k.tj; qa.ntiles = (nstar + k.tj - 1) / k.tj;
     qa.gsplit = k.gsplit; qa.eps2 = eps2;
     if (timed) CU(cudaEventRecord(c->ev0, s));
@@ -397,8 +421,16 @@ extern "C" int pn_force_device(pn_ctx *c, int n, const double *d_x, const double
 }
 
 // Enqueue one integration step (three evaluations with fused stage updates).
+static int step_evaluations(const pn_ctx *c) { return c->p.integrator == PN_INT_RK4 ? 4 : 3; }
+
 static int enqueue_step(pn_ctx *c, cudaStream_t s) {
     const long long ld = c->ld;
+    if (c->p.integrator == PN_INT_RK4) {  // classic RK4: evaluations at y, y2, y3, y4
+        int rc = eval_force(c, c->st.x, c->st.v, c->st.m, 1, ld, nullptr, 3, 1, STAGE_RK4_1, s, false, 0);
+        for (int k = 1; k < 4 && !rc; ++k)
+            rc = eval_force(c, c->st.xs, c->st.vs, c->st.m, 1, ld, nullptr, 3, 1, STAGE_RK4_1 + k, s, false, k);
+        return rc;
+    }
     int rc = eval_force(c, c->st.x, c->st.v, c->st.m, 1, ld, nullptr, 3, 1, 1, s, false, 0);
     if (!rc) rc = eval_force(c, c->st.xs, c->st.vs, c->st.m, 1, ld, nullptr, 3, 1, 2, s, false, 1);
     if (!rc) rc = eval_force(c, c->st.xs, c->st.vs, c->st.m, 1, ld, nullptr, 3, 1, 3, s, false, 2);
@@ -523,10 +555,11 @@ static int eval_energy(pn_ctx *c, const double *x, const double *v, const double
     pa.nstar = nstar; pa.npad = c->npad; pa.nfill = (int)round_up(nstar > 0 ? nstar : 1, 256);
     pa.tj = k.tj; pa.f32 = is_f32(c); pa.eps2 = eps2;
     pa.pack = c->pack; pa.torg = c->torg; pa.spos = c->spos;
+    if (pa.f32) { pa.pack2 = c->pack2; pa.ipack = c->ipack; }
     pa.part = c->part; pa.glob = c->glob; pa.ticket = &c->tickets[0];
     CU(launch_prep(pa, s));
     PairArgs qa{};
-    qa.pack = c->pack; qa.torg = c->torg; qa.spos = c->spos; qa.out = c->acc; qa.err = c->err;
+    qa.pack = c->pack; qa.torg = c->torg; qa.spos = c->spos; qa.pack2 = c->pack2; qa.ipack = c->ipack; qa.out = c->acc; qa.err = c->err;
     qa.nstar = nstar; qa.npad = c->npad; qa.tj = k.tj; qa.ntiles = (nstar + k.tj - 1) / k.tj;
     qa.gsplit = k.gsplit; qa.eps2 = eps2;
     if (nstar > 0) {
@@ -760,7 +793,7 @@ extern "C" int pn_bench_steps(pn_ctx *c, int nsteps, int flush_l2, double *step_
         CU(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
         step_ms[k] = ms;
         double pm = 0.0;
-        for (int q = 0; q < 3; ++q) {
+        for (int q = 0; q < step_evaluations(c); ++q) {
             CU(cudaEventElapsedTime(&ms, c->evp[2 * q], c->evp[2 * q + 1]));
             pm += ms;
         }
@@ -868,10 +901,11 @@ extern "C" int pn_autotune(pn_ctx *c, int sweeps, double *best_ms) {
             pa.nstar = nstar; pa.npad = c->npad; pa.nfill = (int)round_up(nstar, 256);
             pa.tj = k.tj; pa.f32 = f32; pa.eps2 = eps2;
             pa.pack = c->pack; pa.torg = c->torg; pa.spos = c->spos;
+    if (pa.f32) { pa.pack2 = c->pack2; pa.ipack = c->ipack; }
             pa.part = c->part; pa.glob = c->glob; pa.ticket = &c->tickets[0];
             CU(launch_prep(pa, c->stream));
             PairArgs qa{};
-            qa.pack = c->pack; qa.torg = c->torg; qa.spos = c->spos; qa.out = c->acc; qa.err = c->err;
+            qa.pack = c->pack; qa.torg = c->torg; qa.spos = c->spos; qa.pack2 = c->pack2; qa.ipack = c->ipack; qa.out = c->acc; qa.err = c->err;
             qa.nstar = nstar; qa.npad = c->npad; qa.tj = k.tj; qa.ntiles = (nstar + k.tj - 1) / k.tj;
             qa.gsplit = k.gsplit; qa.eps2 = eps2;
             float t = 1e30f;
@@ -887,8 +921,8 @@ extern "C" int pn_autotune(pn_ctx *c, int sweeps, double *best_ms) {
                 if (rep > 0) t = ms;
             }
             if (getenv("PN_TUNE_VERBOSE"))
-                fprintf(stderr, "pn_autotune mode %d: ipt %d js %d tj %d gsplit %d: %.3f ms\n", mode, k.ipt,
-                        k.js, k.tj, k.gsplit, t);
+                fprintf(stderr, "pn_autotune mode %d: ipt %d js %d tj %d gsplit %d x2 %d: %.3f ms\n", mode,
+                        k.ipt, k.js, k.tj, k.gsplit, k.x2, t);
             if (t < best_t) {
                 best_t = t;
                 best = k;

@@ -21,6 +21,8 @@ struct pn_ctx {
     double *in_aos = nullptr;     // [2][ld][3] + [ld] device AoS x, v, m staging (drop-ins)
     double *spos = nullptr;
     void *pack = nullptr;
+    float4 *pack2 = nullptr;      // paired pack of the f32x2 sweep [7][npad/2]
+    float4 *ipack = nullptr;      // [npad] (v.xyz, qe)
     pn::TileOrigin *torg = nullptr;
     double *acc = nullptr;
     int acc_splits = 0;
@@ -36,7 +38,7 @@ struct pn_ctx {
     cudaGraphExec_t step_exec = nullptr;
     bool step_valid = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
-    cudaEvent_t evp[6] = {};      // around the three pair launches of a captured step
+    cudaEvent_t evp[8] = {};      // around the pair launches of a captured step (3, or 4 for RK4)
     void *flush = nullptr;        // L2 flush buffer (benchmarks only)
     size_t flush_bytes = 0;
     pn_stats stats{};

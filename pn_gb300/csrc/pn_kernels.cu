@@ -153,6 +153,23 @@ __device__ __forceinline__ void prep_body(const PrepArgs &a, int blk, int nblk) 
             pk[a.npad + j] = make_float4(lo[0], lo[1], lo[2], (float)mu3);
             pk[2 * a.npad + j] = make_float4((float)vv[0], (float)vv[1], (float)vv[2], (float)qe);
             pk[3 * a.npad + j] = make_float4((float)c1, (float)c3, (float)k35, 0.f);
+            if (a.pack2) {  // paired layout: star j is lane (j & 1) of pair j / 2
+                const int lane = j & 1;
+                const size_t prow = (size_t)a.npad / 2;
+                float *p2 = reinterpret_cast<float *>(a.pack2 + j / 2);
+                const float vals[7][2] = {{hi[0], hi[1]},
+                                          {hi[2], (float)mj},
+                                          {lo[0], lo[1]},
+                                          {lo[2], (float)mu3},
+                                          {(float)vv[0], (float)vv[1]},
+                                          {(float)vv[2], (float)c1},
+                                          {(float)c3, (float)k35}};
+                for (int g = 0; g < 7; ++g) {
+                    p2[g * prow * 4 + lane] = vals[g][0];
+                    p2[g * prow * 4 + 2 + lane] = vals[g][1];
+                }
+                a.ipack[j] = make_float4((float)vv[0], (float)vv[1], (float)vv[2], (float)qe);
+            }
             if (j % a.tj == 0 && real) a.torg[j / a.tj] = TileOrigin{s[0], s[1], s[2], 0.0};
         } else {
             double2 *pk = static_cast<double2 *>(a.pack);
@@ -198,7 +215,27 @@ __device__ __forceinline__ void stage_update(const FinishArgs &a, int p, const d
     for (int k = 0; k < 3; ++k) {
         const size_t o = (size_t)k * a.ld + p;
         const double x = a.st.x[o], v = a.st.v[o];
-        if (a.stage == 1) {  // :853-860
+        if (a.stage >= STAGE_RK4_1) {
+            // classic fourth-order Runge-Kutta (optional integrator; hx, hv accumulate
+            // k1 + 2 k2 + 2 k3 of the position and velocity slopes)
+            if (a.stage == STAGE_RK4_1) {
+                a.st.xs[o] = x + 0.5 * dt * v;
+                a.st.vs[o] = v + 0.5 * dt * acc3[k];
+                a.st.hx[o] = v;
+                a.st.hv[o] = acc3[k];
+            } else if (a.stage == STAGE_RK4_4) {
+                const double vprev = a.st.vs[o];
+                a.st.x[o] = x + (dt / 6.0) * (a.st.hx[o] + vprev);
+                a.st.v[o] = v + (dt / 6.0) * (a.st.hv[o] + acc3[k]);
+            } else {
+                const double vprev = a.st.vs[o];
+                const double f = a.stage == STAGE_RK4_2 ? 0.5 * dt : dt;
+                a.st.xs[o] = x + f * vprev;
+                a.st.vs[o] = v + f * acc3[k];
+                a.st.hx[o] += 2.0 * vprev;
+                a.st.hv[o] += 2.0 * acc3[k];
+            }
+        } else if (a.stage == 1) {  // :853-860
             const double x1 = __dadd_rn(x, __dmul_rn(__dmul_rn(0.5, v), dt));
             const double v1 = __dadd_rn(v, __dmul_rn(__dmul_rn(0.5, acc3[k]), dt));
             a.st.xs[o] = x1;

@@ -5,6 +5,10 @@
 
 namespace pn {
 
+// Stage codes of the optional classic fourth-order Runge-Kutta integrator (the reference's own
+// scheme, Limit-sticky9.c:844-893, uses stages 1..3).
+enum RK4Stage : int { STAGE_RK4_1 = 11, STAGE_RK4_2 = 12, STAGE_RK4_3 = 13, STAGE_RK4_4 = 14 };
+
 // Global per-evaluation sums (FP64) written by k_prep.
 enum GlobSlot : int { G_A1 = 0, G_B3X, G_B3Y, G_B3Z, G_C, G_PX, G_PY, G_PZ, NGLOB };
 constexpr int NACC_MAX = 9;
@@ -30,6 +34,8 @@ struct PrepArgs {
     double *spos;
     double *part, *glob;
     unsigned *ticket;
+    float4 *pack2;  // optional (FP32): paired pack [7][npad/2] of the f32x2 sweep
+    float4 *ipack;  // optional (FP32): [npad] (v.xyz, qe)
 };
 
 struct FinishArgs {
@@ -41,7 +47,7 @@ struct FinishArgs {
     double eps, eps2, inv_c2, dt;
     double *a;            // output acceleration (may be null), [p*asp + k*ask]
     long long asp, ask;
-    int stage;            // 0: none; 1..3: fused integration stage update on st
+    int stage;            // 0: none; 1..3: the reference's stages; STAGE_RK4_1..4: classic RK4
     double *sums_out;     // optional [nacc][npad]: the per-star pair sums (adjoint reuse)
     DevState st;
     long long ld;

@@ -32,6 +32,8 @@ template <> struct PackVec<double> { using V = double2; };
 struct PairArgs {
     const void *pack;     // [NG][npad] of PackVec<T>::V
     const TileOrigin *torg;  // FP32 only: per-tile FP64 origin (BH-relative), one per tile of tj
+    const void *pack2;       // FP32 only: the paired pack of the f32x2 sweep (pn_pair2.cuh)
+    const float4 *ipack;     // FP32 only: per star (v.xyz, qe), the f32x2 sweep's i-side data
     const double *spos;   // [3][npad] BH-relative FP64 positions
     double *out;          // [gsplit][NACC][npad]
     int *err;             // device error word

@@ -1,0 +1,273 @@
+// pn_pair2.cuh -- the FP32 pair sweep on packed FP32x2 instructions (sm_100+ f32x2 PTX).
+//
+// Same sweeps and the same arithmetic per pair as k_pair<float, MODE> (pn_pair.cuh), but every
+// instruction works on TWO j-stars at once: lane 0 of an f32x2 register holds star 2k of the
+// tile, lane 1 star 2k+1, while the i-particle's values are broadcast to both lanes once per
+// tile.  A pair then costs about half the issue slots (the FMA pipe still does the same work),
+// which lifts the sweep from issue-bound to FMA-pipe-bound.  The MUFU rsqrt has no paired form
+// and runs once per lane.
+//
+// j-data come from the "paired" pack (written by k_prep in mixed precision): for star pair k
+// of a tile, 7 float4 groups, group-major over pairs ([g][npad/2]):
+//   P0 (hx hx' hy hy')  P1 (hz hz' m m')  P2 (lx lx' ly ly')  P3 (lz lz' mu3 mu3')
+//   P4 (vx vx' vy vy')  P5 (vz vz' c1 c1')  P6 (c3 c3' k35 k35')
+// (primed = odd star), so one 128-bit shared load yields two f32x2 operands.
+#pragma once
+
+#include "pn_pair.cuh"
+
+namespace pn {
+
+typedef unsigned long long f2;  // two FP32 values in one 64-bit register pair
+
+__device__ __forceinline__ f2 f2_pack(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 f2_bcast(float v) { return f2_pack(v, v); }
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ void lds2(const void *p, f2 &a, f2 &b) {
+    asm volatile("ld.shared.v2.b64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "r"(smem_u32(p)));
+}
+// rsqrt of both lanes (MUFU each) refined by one Newton-Raphson step in f32x2:
+// y' = y (1.5 - 0.5 x y^2).
+__device__ __forceinline__ f2 rsqrt2(f2 x) {
+    float a, b;
+    f2_unpack(x, a, b);
+    float ya, yb;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(ya) : "f"(a));
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yb) : "f"(b));
+    const f2 y = f2_pack(ya, yb);
+    const f2 nxh = mul2(x, f2_bcast(-0.5f));
+    const f2 r = fma2(nxh, mul2(y, y), f2_bcast(1.5f));
+    return mul2(y, r);
+}
+__device__ __forceinline__ float f2_sum(f2 v) {
+    float a, b;
+    f2_unpack(v, a, b);
+    return a + b;
+}
+
+struct I2 {  // one i-particle, broadcast to both lanes
+    f2 ex, ey, ez, lx, ly, lz, vx, vy, vz, vi2, qe;
+};
+
+template <int MODE>
+__device__ __forceinline__ void pair2_accumulate(f2 *acc, const I2 &I, f2 jx, f2 jy, f2 jz, f2 jlx, f2 jly,
+                                                 f2 jlz, f2 jm, f2 jvx, f2 jvy, f2 jvz, f2 jmu3, f2 jc1,
+                                                 f2 jc3, f2 jk35, f2 eps2) {
+    const f2 dx = add2(sub2(jx, I.ex), sub2(jlx, I.lx));
+    const f2 dy = add2(sub2(jy, I.ey), sub2(jly, I.ly));
+    const f2 dz = add2(sub2(jz, I.ez), sub2(jlz, I.lz));
+    const f2 rhoe = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, eps2)));
+    const f2 Q = rsqrt2(rhoe);
+    const f2 Q2 = mul2(Q, Q);
+    const f2 mQ = mul2(jm, Q);
+    if constexpr (MODE == MODE_NEWTON) {
+        const f2 mQ3 = mul2(mQ, Q2);
+        acc[A_GX] = fma2(mQ3, dx, acc[A_GX]);
+        acc[A_GY] = fma2(mQ3, dy, acc[A_GY]);
+        acc[A_GZ] = fma2(mQ3, dz, acc[A_GZ]);
+    } else if constexpr (MODE == MODE_FORCE) {
+        const f2 mQ3 = mul2(mQ, Q2);
+        acc[A_GX] = fma2(mQ3, dx, acc[A_GX]);
+        acc[A_GY] = fma2(mQ3, dy, acc[A_GY]);
+        acc[A_GZ] = fma2(mQ3, dz, acc[A_GZ]);
+        acc[A_PHI] = add2(acc[A_PHI], mQ);
+        acc[A_S0] = add2(acc[A_S0], mQ3);
+        const f2 uQ = mul2(jmu3, Q);
+        acc[A_U] = add2(acc[A_U], uQ);
+        const f2 dvx = sub2(jvx, I.vx), dvy = sub2(jvy, I.vy), dvz = sub2(jvz, I.vz);
+        const f2 dv2 = fma2(dvz, dvz, fma2(dvy, dvy, mul2(dvx, dvx)));
+        const f2 vdj = fma2(jvz, dz, fma2(jvy, dy, mul2(jvx, dx)));
+        const f2 vdi = fma2(I.vz, dz, fma2(I.vy, dy, mul2(I.vx, dx)));
+        f2 br = fma2(sub2(rhoe, I.qe), jc3, jc1);
+        br = add2(br, fma2(f2_bcast(-2.f), dv2, I.vi2));
+        br = fma2(f2_bcast(1.5f), mul2(mul2(vdj, vdj), Q2), br);
+        const f2 cd = fma2(mQ3, br, mul2(jk35, Q));
+        const f2 cv = mul2(mQ3, fma2(f2_bcast(4.f), vdi, mul2(f2_bcast(-3.f), vdj)));
+        acc[A_WX] = fma2(cd, dx, fma2(cv, dvx, acc[A_WX]));
+        acc[A_WY] = fma2(cd, dy, fma2(cv, dvy, acc[A_WY]));
+        acc[A_WZ] = fma2(cd, dz, fma2(cv, dvz, acc[A_WZ]));
+    } else {  // MODE_ENERGY
+        acc[E_PHI] = add2(acc[E_PHI], mQ);
+        const f2 vivj = fma2(I.vz, jvz, fma2(I.vy, jvy, mul2(I.vx, jvx)));
+        const f2 vdj = fma2(jvz, dz, fma2(jvy, dy, mul2(jvx, dx)));
+        const f2 vdi = fma2(I.vz, dz, fma2(I.vy, dy, mul2(I.vx, dx)));
+        acc[E_PSI] = fma2(mQ, fma2(f2_bcast(7.f), vivj, mul2(mul2(vdi, vdj), Q2)), acc[E_PSI]);
+    }
+}
+
+template <int MODE> struct Mode2 {
+    static constexpr int NG = MODE == MODE_NEWTON ? 4 : (MODE == MODE_FORCE ? 7 : 6);
+};
+
+template <int MODE, int IPT>
+constexpr int pair2_min_blocks() {
+    return IPT == 1 ? 4 : 2;
+}
+
+// One work item of the paired sweep: the i-block at ibase (128 * IPT stars) against j-range
+// `split`.  As pair_block (pn_pair.cuh): TMA double-buffered tiles, bounded waits, per-i Kahan
+// folding of each tile's sums, FP64 partial sums out.  a.pack is the paired pack, a.ipack the
+// i-side float4 (v.xyz, qe) array.
+template <int MODE, int IPT>
+__device__ __forceinline__ bool pair2_block(const PairArgs &a, int ibase, int split, uint64_t *bars,
+                                            float4 *buf, uint32_t &seq) {
+    constexpr int NT = PAIR_NT;
+    constexpr int NG = Mode2<MODE>::NG;
+    constexpr int NACC = ModeInfo<MODE>::NACC;
+    const int tid = threadIdx.x;
+    const int t0 = (int)(((long long)a.ntiles * split) / a.gsplit);
+    const int t1 = (int)(((long long)a.ntiles * (split + 1)) / a.gsplit);
+    const int tj = a.tj, tp = tj / 2;  // stars and star pairs per tile
+    const int prow = a.npad / 2;       // row stride of the paired pack, in float4
+    const float4 *pack = static_cast<const float4 *>(a.pack);
+    const f2 eps2 = f2_bcast((float)a.eps2);
+
+    I2 I[IPT];
+    double sx[IPT], sy[IPT], sz[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int i = ibase + tid + k * NT;
+        const bool valid = i < a.nstar;
+        sx[k] = valid ? a.spos[i] : 0.0;
+        sy[k] = valid ? a.spos[a.npad + i] : 0.0;
+        sz[k] = valid ? a.spos[2 * a.npad + i] : 0.0;
+        float vx = 0.f, vy = 0.f, vz = 0.f, qe = 0.f;
+        if (MODE != MODE_NEWTON && valid) {
+            const float4 g = a.ipack[i];
+            vx = g.x; vy = g.y; vz = g.z; qe = g.w;
+        }
+        I[k].vx = f2_bcast(vx);
+        I[k].vy = f2_bcast(vy);
+        I[k].vz = f2_bcast(vz);
+        I[k].qe = f2_bcast(qe);
+        I[k].vi2 = f2_bcast(fmaf(vz, vz, fmaf(vy, vy, vx * vx)));
+    }
+    float run[IPT][NACC], cmp[IPT][NACC];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k)
+#pragma unroll
+        for (int q = 0; q < NACC; ++q) run[k][q] = cmp[k][q] = 0.f;
+
+    const uint32_t gbytes = (uint32_t)tp * 16u;
+    auto issue = [&](int t, int stage) {
+        mbar_arrive_expect_tx(&bars[stage], (uint32_t)NG * gbytes);
+#pragma unroll
+        for (int g = 0; g < NG; ++g)
+            bulk_g2s(buf + (size_t)(stage * NG + g) * tp, pack + (size_t)g * prow + (size_t)t * tp, gbytes,
+                     &bars[stage]);
+    };
+    if (tid == 0 && t0 < t1) issue(t0, (int)(seq & 1u));
+
+    for (int t = t0; t < t1; ++t) {
+        const uint32_t it = seq + (uint32_t)(t - t0);
+        const int stage = (int)(it & 1u);
+        const uint32_t phase = (it >> 1) & 1u;
+        const bool next = (t + 1 < t1);
+        if (tid == 0 && next) issue(t + 1, stage ^ 1);
+        const bool ok = mbar_wait_bounded(&bars[stage], phase);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicOr(a.err, DEVERR_TIMEOUT);
+                mbar_wait_bounded(&bars[stage], phase);
+                if (next) mbar_wait_bounded(&bars[stage ^ 1], ((it + 1) >> 1) & 1u);
+            }
+            return false;
+        }
+        {
+            const TileOrigin o = a.torg[t];
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const double rx = sx[k] - o.x, ry = sy[k] - o.y, rz = sz[k] - o.z;
+                const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
+                I[k].ex = f2_bcast(hx);
+                I[k].ey = f2_bcast(hy);
+                I[k].ez = f2_bcast(hz);
+                I[k].lx = f2_bcast((float)(rx - (double)hx));
+                I[k].ly = f2_bcast((float)(ry - (double)hy));
+                I[k].lz = f2_bcast((float)(rz - (double)hz));
+            }
+        }
+        const float4 *b = buf + (size_t)stage * NG * tp;
+        f2 tacc[IPT][NACC];
+#pragma unroll
+        for (int k = 0; k < IPT; ++k)
+#pragma unroll
+            for (int q = 0; q < NACC; ++q) tacc[k][q] = 0ull;  // +0.0f in both lanes
+
+#pragma unroll 2
+        for (int jp = 0; jp < tp; ++jp) {
+            f2 jx, jy, jz, jm, jlx, jly, jlz, jmu3, jvx = 0, jvy = 0, jvz = 0, jc1 = 0, jc3 = 0, jk35 = 0;
+            lds2(b + jp, jx, jy);
+            lds2(b + tp + jp, jz, jm);
+            lds2(b + 2 * tp + jp, jlx, jly);
+            lds2(b + 3 * tp + jp, jlz, jmu3);
+            if constexpr (MODE != MODE_NEWTON) {
+                lds2(b + 4 * tp + jp, jvx, jvy);
+                lds2(b + 5 * tp + jp, jvz, jc1);
+            }
+            if constexpr (MODE == MODE_FORCE) lds2(b + 6 * tp + jp, jc3, jk35);
+#pragma unroll
+            for (int k = 0; k < IPT; ++k)
+                pair2_accumulate<MODE>(tacc[k], I[k], jx, jy, jz, jlx, jly, jlz, jm, jvx, jvy, jvz, jmu3, jc1,
+                                       jc3, jk35, eps2);
+        }
+#pragma unroll
+        for (int k = 0; k < IPT; ++k)
+#pragma unroll
+            for (int q = 0; q < NACC; ++q) kahan_add(run[k][q], cmp[k][q], f2_sum(tacc[k][q]));
+        __syncthreads();
+    }
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int i = ibase + tid + k * NT;
+        if (i < a.nstar)
+#pragma unroll
+            for (int q = 0; q < NACC; ++q)
+                a.out[((size_t)split * NACC + q) * a.npad + i] = (double)run[k][q] - (double)cmp[k][q];
+    }
+    seq += (uint32_t)(t1 - t0 > 0 ? t1 - t0 : 0);
+    return true;
+}
+
+template <int MODE, int IPT>
+__global__ void __launch_bounds__(PAIR_NT, (pair2_min_blocks<MODE, IPT>())) k_pair2(const PairArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    float4 *buf = reinterpret_cast<float4 *>(smem + 128);
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t seq = 0;
+    pair2_block<MODE, IPT>(a, blockIdx.x * (PAIR_NT * IPT), blockIdx.y, bars, buf, seq);
+}
+
+}  // namespace pn

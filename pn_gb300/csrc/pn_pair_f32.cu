@@ -1,7 +1,35 @@
 // pn_pair_f32.cu -- instantiations and launcher of the float pair-sweep kernel (see pn_pair.cuh).
 #include "pn_internal.h"
+#include "pn_pair2.cuh"
 
 namespace pn {
+
+// the packed f32x2 sweep (pn_pair2.cuh) on the paired pack
+template <int MODE, int IPT>
+static cudaError_t launch_two(const PairCfg &c, const PairArgs &a0, cudaStream_t s) {
+    PairArgs a = a0;
+    a.pack = a0.pack2;
+    const size_t smem = 128 + 2 * (size_t)Mode2<MODE>::NG * (size_t)(c.tj / 2) * 16;
+    auto fn = k_pair2<MODE, IPT>;
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    const int bi = PAIR_NT * IPT;
+    dim3 grid((unsigned)((a.nstar + bi - 1) / bi), (unsigned)c.gsplit);
+    fn<<<grid, PAIR_NT, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <int MODE>
+static cudaError_t launch_two_mode(const PairCfg &c, const PairArgs &a, cudaStream_t s) {
+    if (c.js != 1 || !a.pack2 || !a.ipack) return cudaErrorInvalidValue;
+    if (c.ipt == 1) return launch_two<MODE, 1>(c, a, s);
+    if (c.ipt == 2) return launch_two<MODE, 2>(c, a, s);
+    return cudaErrorInvalidValue;
+}
 
 template <int MODE, int IPT, int JS>
 static cudaError_t launch_one(const PairCfg &c, const PairArgs &a, cudaStream_t s) {
@@ -37,6 +65,14 @@ static cudaError_t launch_mode(const PairCfg &c, const PairArgs &a, cudaStream_t
 
 cudaError_t launch_pair_f32(int mode, const PairCfg &c, const PairArgs &a, cudaStream_t s) {
     if (a.nstar <= 0) return cudaSuccess;
+    if (c.x2) {
+        switch (mode) {
+            case MODE_NEWTON: return launch_two_mode<MODE_NEWTON>(c, a, s);
+            case MODE_FORCE: return launch_two_mode<MODE_FORCE>(c, a, s);
+            case MODE_ENERGY: return launch_two_mode<MODE_ENERGY>(c, a, s);
+            default: return cudaErrorInvalidValue;
+        }
+    }
     switch (mode) {
         case MODE_NEWTON: return launch_mode<MODE_NEWTON>(c, a, s);
         case MODE_FORCE: return launch_mode<MODE_FORCE>(c, a, s);

@@ -4,8 +4,8 @@
 // candidate list on real data (CUDA events around the pair launch only, one warm-up launch per
 // shape) and keeps the fastest per key (precision, sweep mode, size class = floor(log2 N)).
 // Results live in a process-wide table; with PN_TUNE_CACHE=<file> they are also read from and
-// appended to a text file ("prec mode class ipt js tj gsplit ms" per line), so a tuned shape
-// is reused by later runs.
+// appended to a text file ("prec mode class ipt js tj gsplit x2 ms" per line), so a tuned
+// shape is reused by later runs.  x2 = 1 selects the packed f32x2 sweep (pn_pair2.cuh).
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -40,10 +40,11 @@ void load_file_locked() {
     FILE *f = fopen(path, "r");
     if (!f) return;
     Entry e{};
-    while (fscanf(f, "%d %d %d %d %d %d %d %lf", &e.prec, &e.mode, &e.cls, &e.cfg.ipt, &e.cfg.js,
-                  &e.cfg.tj, &e.cfg.gsplit, &e.ms) == 8) {
+    while (fscanf(f, "%d %d %d %d %d %d %d %d %lf", &e.prec, &e.mode, &e.cls, &e.cfg.ipt, &e.cfg.js,
+                  &e.cfg.tj, &e.cfg.gsplit, &e.cfg.x2, &e.ms) == 9) {
         if (pair_shape_supported(e.cfg.ipt, e.cfg.js) && e.cfg.gsplit >= 1 && e.cfg.gsplit <= 64 &&
-            (e.cfg.tj == 32 || e.cfg.tj == 64 || e.cfg.tj == 128 || e.cfg.tj == 256))
+            (e.cfg.tj == 32 || e.cfg.tj == 64 || e.cfg.tj == 128 || e.cfg.tj == 256) &&
+            (e.cfg.x2 == 0 || (e.cfg.x2 == 1 && e.cfg.js == 1 && e.cfg.ipt <= 2 && e.prec == 1)))
             g_table.push_back(e);
     }
     fclose(f);
@@ -54,8 +55,8 @@ void append_file_locked(const Entry &e) {
     if (!path) return;
     FILE *f = fopen(path, "a");
     if (!f) return;
-    fprintf(f, "%d %d %d %d %d %d %d %.6f\n", e.prec, e.mode, e.cls, e.cfg.ipt, e.cfg.js, e.cfg.tj,
-            e.cfg.gsplit, e.ms);
+    fprintf(f, "%d %d %d %d %d %d %d %d %.6f\n", e.prec, e.mode, e.cls, e.cfg.ipt, e.cfg.js, e.cfg.tj,
+            e.cfg.gsplit, e.cfg.x2, e.ms);
     fclose(f);
 }
 }  // namespace
@@ -111,7 +112,12 @@ std::vector<PairCfg> tune_candidates(bool f32, int mode, int nstar, int sms) {
             for (int g : gs) {
                 if (g > 1 && g > ntiles / 4) break;  // keep >= 4 tiles per j-range
                 c.gsplit = g;
+                c.x2 = 0;
                 out.push_back(c);
+                if (f32 && js == 1 && ipt <= 2) {  // the packed f32x2 sweep of the same shape
+                    c.x2 = 1;
+                    out.push_back(c);
+                }
             }
         }
     }

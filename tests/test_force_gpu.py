@@ -117,7 +117,10 @@ def test_config1_uniform_sphere_100_steps(pn):
 # ------------------------------------------------------------------ against the oracle
 SHAPES = [dict(), dict(i_per_thread=1), dict(i_per_thread=4), dict(j_split=2), dict(j_split=4),
           dict(j_split=8), dict(tile_j=32), dict(tile_j=256), dict(grid_split=3),
-          dict(grid_split=7, tile_j=32, j_split=4)]
+          dict(grid_split=7, tile_j=32, j_split=4),
+          # the packed f32x2 sweep (mixed precision only; FP64 ignores the variant)
+          dict(pair_variant=2), dict(pair_variant=2, i_per_thread=1, tile_j=32),
+          dict(pair_variant=2, i_per_thread=2, tile_j=256, grid_split=5)]
 
 
 @pytest.mark.parametrize("n", [1, 2, 3, 33, 64, 65, 129, 257, 1000])
@@ -188,13 +191,23 @@ def test_deterministic(pn):
             assert np.array_equal(c.force(), c.force())
 
 
-def test_newtonian_only(pn, oracle):
+@pytest.mark.parametrize("variant", [0, 2])
+def test_newtonian_only(pn, oracle, variant):
     """inv_c2 = 0 gives the Newtonian sweep alone (Limit-sticky9.c:36-51)."""
     x, v, m = random_system(700, 9)
     an = oracle.force_newton(x, m, 0.02)
     assert relerr(ctx_force(pn, x, v, m, 0.02, inv_c2=0.0), an).max() <= TOL_A
-    e = relerr(ctx_force(pn, x, v, m, 0.02, inv_c2=0.0, precision=1), an)
+    e = relerr(ctx_force(pn, x, v, m, 0.02, inv_c2=0.0, precision=1, pair_variant=variant), an)
     assert np.sqrt((e ** 2).mean()) <= 1e-6
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_mixed_energy_sweep(pn, oracle, variant):
+    x, v, m = random_system(900, 14, v0=0.05)
+    with pn.Context(900, eps=0.02, precision=1, pair_variant=variant) as c:
+        c.set_state(x, v, m)
+        e = np.array(c.energy())
+    assert np.abs(e / oracle.energy(x, v, m, 0.02) - 1).max() <= 1e-6
 
 
 @pytest.mark.parametrize("cval", [10.0, 1000.0])
@@ -313,3 +326,45 @@ def test_mixed_energy_drift_matches_fp64(pn):
             c.steps(50)
             drift.append(c.energy()[3] / e0 - 1)
     assert abs(drift[1] - drift[0]) <= 1e-6 + 0.05 * abs(drift[0])
+
+
+# ------------------------------------------------------------------ optional classic RK4
+def test_rk4_matches_host_rk4_with_oracle_forces(pn, oracle):
+    x, v, m = random_system(120, 31)
+    eps, h = 0.02, 2e-3
+
+    def f(xx, vv):
+        return vv, oracle.force_exact(xx, vv, m, eps)
+
+    xr, vr = x.copy(), v.copy()
+    for _ in range(3):
+        k1x, k1v = f(xr, vr)
+        k2x, k2v = f(xr + 0.5 * h * k1x, vr + 0.5 * h * k1v)
+        k3x, k3v = f(xr + 0.5 * h * k2x, vr + 0.5 * h * k2v)
+        k4x, k4v = f(xr + h * k3x, vr + h * k3v)
+        xr = xr + h / 6 * (k1x + 2 * k2x + 2 * k3x + k4x)
+        vr = vr + h / 6 * (k1v + 2 * k2v + 2 * k3v + k4v)
+    with pn.Context(120, eps=eps, dt=h, integrator=1) as c:
+        c.set_state(x, v, m)
+        c.steps(3)
+        xg, vg = c.get_state()
+    assert traj_err(xg, xr) <= 1e-12 and traj_err(vg, vr) <= 1e-12
+
+
+def test_rk4_is_fourth_order(pn):
+    """Newtonian two-body orbit (inv_c2 = 0): halving dt divides the RK4 error by ~16, while
+    the reference's state-averaging scheme is first order (error halves)."""
+    x = np.array([[0.0, 0, 0], [1.0, 0, 0]])
+    v = np.array([[0.0, 0, 0], [0, 1.0, 0]])
+    m = np.array([1.0, 1e-12])
+
+    def end(integrator, dt, steps):
+        with pn.Context(2, eps=1e-4, dt=dt, inv_c2=0.0, integrator=integrator) as c:
+            c.set_state(x, v, m)
+            c.steps(steps)
+            return c.get_state()[0][1]
+
+    exact = end(1, 1e-3 / 8, 1600)  # t = 0.2 with a small step as the reference solution
+    e1 = np.abs(end(1, 1e-2, 20) - exact).max()
+    e2 = np.abs(end(1, 5e-3, 40) - exact).max()
+    assert 12 < e1 / e2 < 20
