@@ -338,6 +338,33 @@ def run_adjoint(args):
     return 0
 
 
+def run_long(args, nstars, precisions, nsteps_by_prec, label):
+    """Energy drift and step throughput of device-resident runs (one JSON line)."""
+    import pn_gb300 as pn
+    s = pn.config_plummer(nstars, SEED, BH_FRACTION)
+    eps = pn.plummer_eps(nstars)
+    n = nstars + 1
+    res = {}
+    for prec in precisions:
+        with pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=0) as c:
+            c.set_state(s.x, s.v, s.m)
+            e0 = c.energy()[3]  # energies in FP64 for both modes
+            c.set_params(precision=prec)
+            k = nsteps_by_prec[prec]
+            with ClockSampler() as clk:
+                ms = c.bench_steps(k, flush_l2=False)[0]
+            c.set_params(precision=0)
+            e1 = c.energy()[3]
+            res["mixed" if prec else "fp64"] = {
+                "steps": k, "ms_per_step": float(ms.mean()), "value": 3.0 * n * n / (ms.mean() * 1e-3),
+                "energy_drift": float(e1 / e0 - 1), "drift_per_step": float((e1 / e0 - 1) / k),
+                "clocks": clk.summary()}
+    line = {"metric": label, "unit": UNIT, "n_gpus": 1, "data": "synthetic",
+            "config": dict(workload_config(nstars), dt=DT), **res}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def profile_case(nstars):
     """One mixed-precision force evaluation of the bench workload at nstars (ncu target)."""
     import pn_gb300 as pn
@@ -387,7 +414,17 @@ def main():
     ap.add_argument("--adj-n", type=int, default=16384)
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--fd-coords", type=int, default=2)
+    ap.add_argument("--fp64-run", type=int, default=0, metavar="STEPS",
+                    help="FP64 Plummer run at N=65536 for STEPS steps (throughput, energy drift)")
+    ap.add_argument("--drift", type=int, default=0, metavar="STEPS",
+                    help="energy drift of the headline workload: mixed for STEPS, FP64 for STEPS/20")
     args = ap.parse_args()
+    if args.fp64_run:
+        return run_long(args, 65536, (0,), {0: args.fp64_run},
+                        "FP64 integration at N=65536 (interactions/s, energy drift)")
+    if args.drift:
+        return run_long(args, args.nstars, (1, 0), {1: args.drift, 0: max(1, args.drift // 20)},
+                        "energy drift, mixed vs FP64 (interactions/s per mode)")
     if args.profile_case:
         return profile_case(args.profile_case)
     if args.ensemble:
