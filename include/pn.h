@@ -172,6 +172,25 @@ int pn_probe_fma_peak(int precision, double *tflops);
  * worked and the kernel returned on its own.  Faults nothing; the context stays usable. */
 int pn_selftest_wait_timeout(pn_ctx *ctx, double seconds);
 
+/* A force evaluation that allocates nothing.  No counterpart in the reference (its force()
+ * allocates a 6.5 MB stack array per call).  For callers that cannot call cudaMalloc when they
+ * need a force: a framework that owns all device memory through its own pool, a time-critical
+ * loop in which cudaMalloc/cudaFree would stall the device, a plug-in host that forbids
+ * allocation after start-up.  The caller passes device arrays d_x, d_v (AoS double[n][3]),
+ * d_m (double[n]) and the output d_a (double[n][3]); precision is PN_PREC_FP64 or
+ * PN_PREC_MIXED; stream is a cudaStream_t (NULL = the default stream) and the call is
+ * asynchronous on it.  All work buffers live in one fixed device array of
+ * PN_NOALLOC_SCRATCH_BYTES inside the library, held by every GPU that loads it until the
+ * process exits, so n may not exceed PN_NOALLOC_NMAX (PN_ERR_INVALID otherwise).  The first call
+ * on a device looks up that array's device address (make it before any stream capture).  Calls
+ * share the array: calls that overlap on the GPU race.  Device-side problems (a non-finite
+ * force) are not reported back; they show in d_a. */
+#define PN_NOALLOC_NMAX 8192
+#define PN_NOALLOC_SCRATCH_BYTES 3355904
+int pn_force_noalloc(int n, const double *d_x, const double *d_v, const double *d_m, double eps,
+                     double inv_c2, int precision, double *d_a, void *stream);
+int pn_noalloc_last_error(void);
+
 /* ------------------------------------------------------------------ 2a. discrete adjoint */
 /* Vector-Jacobian product of one force evaluation at the current state: for abar (host AoS
  * [n][3], the adjoint of the accelerations) returns xbar = (da/dx)^T abar, vbar = (da/dv)^T
