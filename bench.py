@@ -365,18 +365,23 @@ def run_long(args, nstars, precisions, nsteps_by_prec, label):
     return 0
 
 
-def profile_case(nstars):
-    """One mixed-precision force evaluation of the bench workload at nstars (ncu target)."""
+def profile_case(nstars, shape=None):
+    """One mixed-precision force evaluation of the bench workload at nstars (ncu target);
+    shape = "ipt,tile_j,grid_split" pins the packed sweep's launch shape (e.g. the tuned one)."""
     import pn_gb300 as pn
     sysm = pn.config_plummer(nstars, SEED, BH_FRACTION)
+    kw = {}
+    if shape:
+        ipt, tj, gs = (int(t) for t in shape.split(","))
+        kw = dict(i_per_thread=ipt, tile_j=tj, grid_split=gs, pair_variant=2)
     with pn.Context(nstars + 1, eps=pn.plummer_eps(nstars), inv_c2=INV_C2,
-                    precision=pn.PN_PREC_MIXED) as c:
+                    precision=pn.PN_PREC_MIXED, **kw) as c:
         c.set_state(sysm.x, sysm.v, sysm.m)
         c.force()
         st = c.stats()
         print(json.dumps({"profile_case": nstars, "pair_ms": st.pair_ms, "tile_j": st.tile_j,
                           "i_per_thread": st.i_per_thread, "j_split": st.j_split,
-                          "grid_split": st.grid_split}))
+                          "grid_split": st.grid_split, "pair_variant": st.pair_variant}))
     return 0
 
 
@@ -414,6 +419,7 @@ def main():
     ap.add_argument("--adj-n", type=int, default=16384)
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--fd-coords", type=int, default=2)
+    ap.add_argument("--shape", default=None, help="--profile-case launch shape: ipt,tile_j,grid_split")
     ap.add_argument("--fp64-run", type=int, default=0, metavar="STEPS",
                     help="FP64 Plummer run at N=65536 for STEPS steps (throughput, energy drift)")
     ap.add_argument("--drift", type=int, default=0, metavar="STEPS",
@@ -426,7 +432,7 @@ def main():
         return run_long(args, args.nstars, (1, 0), {1: args.drift, 0: max(1, args.drift // 20)},
                         "energy drift, mixed vs FP64 (interactions/s per mode)")
     if args.profile_case:
-        return profile_case(args.profile_case)
+        return profile_case(args.profile_case, args.shape)
     if args.ensemble:
         return run_ensemble(args)
     if args.adjoint:
@@ -481,7 +487,8 @@ def main():
         peak32 = pn.probe_fma_peak(pn.PN_PREC_MIXED)
         pairs = float(ns) * float(ns)
         achieved = pairs * flops_pair / (pair_launch_ms * 1e-3) / 1e12
-        line["roofline"] = {"bound": "fp32", "kernel": "k_pair<float, MODE_FORCE>",
+        kname = "k_pair2<MODE_FORCE> (packed f32x2)" if st.pair_variant == 2 else "k_pair<float, MODE_FORCE>"
+        line["roofline"] = {"bound": "fp32", "kernel": kname,
                             "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                             "frac": achieved / peak32, "traffic": None,
                             "flops_per_pair": flops_pair,

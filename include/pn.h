@@ -87,6 +87,7 @@ typedef struct {
     double total_ms;         /* whole force evaluation */
     double interactions;     /* star-star pairs evaluated by that launch */
     int tile_j, i_per_thread, j_split, grid_split, threads; /* launch shape used */
+    int pair_variant;        /* PN_PAIR_SCALAR or PN_PAIR_F32X2: the pair kernel used */
 } pn_stats;
 
 /* ------------------------------------------------------------------ 1. drop-in entry points */
@@ -129,6 +130,12 @@ int pn_steps(pn_ctx *ctx, int nsteps);
 int pn_sync(pn_ctx *ctx);
 /* Energies of the current state (Limit-sticky9.c:445-556 arithmetic). */
 int pn_energy(pn_ctx *ctx, pn_energy_t *e);
+/* The energies of the current state, as pn_energy, and then nsteps (>= 1) integration steps,
+ * as pn_steps: the energy's pair sums are accumulated by the first step's first force sweep,
+ * which runs at that same state, so a snapshot's energy costs no sweep of its own (the
+ * reference's main loop evaluates initial_energy() or energy() and then force() at the same
+ * state, Limit-sticky9.c:837 or :896, then :851).  Waits for the steps, like pn_sync. */
+int pn_steps_energy(pn_ctx *ctx, int nsteps, pn_energy_t *e);
 double pn_time(pn_ctx *ctx);
 int pn_get_stats(pn_ctx *ctx, pn_stats *s);
 /* Changes the run parameters of an existing context (e.g. precision). */

@@ -61,7 +61,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("pair_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
                 ("interactions", ctypes.c_double), ("tile_j", ctypes.c_int),
                 ("i_per_thread", ctypes.c_int), ("j_split", ctypes.c_int),
-                ("grid_split", ctypes.c_int), ("threads", ctypes.c_int)]
+                ("grid_split", ctypes.c_int), ("threads", ctypes.c_int),
+                ("pair_variant", ctypes.c_int)]
 
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -88,6 +89,7 @@ SIGNATURES = [
     ("pn_steps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     ("pn_sync", ctypes.c_int, [ctypes.c_void_p]),
     ("pn_energy", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Energy)]),
+    ("pn_steps_energy", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Energy)]),
     ("pn_time", ctypes.c_double, [ctypes.c_void_p]),
     ("pn_get_stats", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
     ("pn_set_params", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Params)]),
@@ -285,6 +287,13 @@ class Context:
     def energy(self):
         e = Energy()
         _check(lib().pn_energy(self._h, ctypes.byref(e)), "pn_energy")
+        return e.as_tuple()
+
+    def steps_energy(self, k: int):
+        """Energies of the current state (as energy()) from the first force sweep of the next
+        k integration steps, which are then run (as steps())."""
+        e = Energy()
+        _check(lib().pn_steps_energy(self._h, int(k), ctypes.byref(e)), "pn_steps_energy")
         return e.as_tuple()
 
     @property

@@ -95,11 +95,21 @@ int main(int argc, char **argv) {
         if (rc) return die("snapshot", rc);
         rc = pn_set_state(ctx, n, x, v, m);
         if (rc) return die("pn_set_state", rc);
-        rc = pn_energy(ctx, &e);                              /* :837 initial_energy */
+        eouttime = time + deouttime;                          /* :828 */
+    }
+    /* An energy owed for the current state (initial_energy at :837, or energy at a snapshot,
+     * :896) is taken from the force sweep that starts the next steps at that same state
+     * (pn_steps_energy) and printed when those steps are done; printed lines and their order
+     * are the reference's.  A run that ends on a snapshot, or that writes checkpoints, uses a
+     * separate energy sweep. */
+    enum { OWE_NONE, OWE_INITIAL, OWE_SNAPSHOT } owed = resume ? OWE_NONE : OWE_INITIAL;
+    double owed_time = 0.0;
+    if (owed == OWE_INITIAL && !(time < endtime)) {
+        rc = pn_energy(ctx, &e);
         if (rc) return die("pn_energy", rc);
         print_energy(0.0, &e, 0, 0.0);
         init_ene = e.total;
-        eouttime = time + deouttime;                          /* :828 */
+        owed = OWE_NONE;
     }
     /* the reference steps until time >= endtime, with a snapshot whenever time >= eouttime
      * (:841-908); steps between snapshots run back to back on the GPU */
@@ -111,21 +121,38 @@ int main(int argc, char **argv) {
             k++;
             if (t >= eouttime) break;
         }
-        rc = pn_steps(ctx, k);
-        if (!rc) rc = pn_sync(ctx);
-        if (rc) return die("pn_steps", rc);
+        if (owed != OWE_NONE) {
+            rc = pn_steps_energy(ctx, k, &e);
+            if (rc) return die("pn_steps_energy", rc);
+            if (owed == OWE_INITIAL) {
+                print_energy(0.0, &e, 0, 0.0);
+                init_ene = e.total;
+            } else {
+                print_energy(owed_time, &e, 1, init_ene);
+            }
+            owed = OWE_NONE;
+        } else {
+            rc = pn_steps(ctx, k);
+            if (!rc) rc = pn_sync(ctx);
+            if (rc) return die("pn_steps", rc);
+        }
         time = t;
         if (time >= eouttime) {                               /* :895-906 */
-            rc = pn_energy(ctx, &e);
-            if (rc) return die("pn_energy", rc);
-            print_energy(time, &e, 1, init_ene);
             eouttime += deouttime;
             rc = pn_get_state(ctx, x, v);
             if (!rc) rc = write_snap(output, n, x, v, lossless);
             if (rc) return die("snapshot", rc);
-            if (ckpt) {
-                rc = pn_save_checkpoint(ctx, ckpt, eouttime, init_ene);
-                if (rc) return die("checkpoint", rc);
+            if (ckpt || !(time < endtime)) {
+                rc = pn_energy(ctx, &e);
+                if (rc) return die("pn_energy", rc);
+                print_energy(time, &e, 1, init_ene);
+                if (ckpt) {
+                    rc = pn_save_checkpoint(ctx, ckpt, eouttime, init_ene);
+                    if (rc) return die("checkpoint", rc);
+                }
+            } else {
+                owed = OWE_SNAPSHOT;
+                owed_time = time;
             }
             fflush(stdout);
         }

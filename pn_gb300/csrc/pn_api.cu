@@ -154,7 +154,8 @@ int pn::ensure_acc(pn_ctx *c, int splits) {
     if (c->acc) cudaFree(c->acc);
     c->acc = nullptr;
     c->acc_splits = 0;
-    size_t bytes = (size_t)splits * NACC_MAX * (size_t)c->npad * sizeof(double);
+    // room for the widest sweep: the force sweep with the fused energy sum
+    size_t bytes = (size_t)splits * pair_nacc(MODE_FORCE_ENERGY) * (size_t)c->npad * sizeof(double);
     if (cudaMalloc(&c->acc, bytes) != cudaSuccess) {
         cudaGetLastError();
         return set_err(PN_ERR_NOMEM, "acc: %zu bytes", bytes);
@@ -278,13 +279,15 @@ void pn::refresh_cfg(pn_ctx *c) {
 
 // One force evaluation.  x, v, m: particle p component k at [p*sp + k*sk] (device).
 // a_out: optional device output (AoS when asp=3, ask=1).  stage: fused integration stage.
+// with_energy: the same sweep also accumulates the energy's Psi, and the energies of the state
+// (x, v) are written to c->eout (the sweep's Phi is the energy's Phi).
 int pn::eval_force(pn_ctx *c, const double *x, const double *v, const double *m, long long sp,
                    long long sk, double *a_out, long long asp, long long ask, int stage,
-                   cudaStream_t s, bool timed, int tslot, double *sums_out) {
+                   cudaStream_t s, bool timed, int tslot, double *sums_out, bool with_energy) {
     const int n = c->n;
     const int nstar = n - 1;
     refresh_cfg(c);
-    const int mode = force_mode(c);
+    const int mode = with_energy ? (int)MODE_FORCE_ENERGY : force_mode(c);
     const PairCfg &k = c->cfg_force;
     int rc = ensure_acc(c, k.gsplit);
     if (rc) return rc;
@@ -312,12 +315,23 @@ int pn::eval_force(pn_ctx *c, const double *x, const double *v, const double *m,
     }
     if (tslot >= 0) CU(cudaEventRecordWithFlags(c->evp[2 * tslot + 1], s, cudaEventRecordExternal));
     if (timed) CU(cudaEventRecord(c->ev1, s));
+    if (with_energy) {
+        EnergyArgs ea{};
+        ea.v = v; ea.m = m; ea.sp = sp; ea.sk = sk;
+        ea.spos = c->spos; ea.acc = c->acc; ea.glob = c->glob;
+        ea.nstar = nstar; ea.npad = c->npad; ea.gsplit = k.gsplit;
+        ea.nacc = pair_nacc(mode); ea.sphi = A_PHI; ea.spsi = A_PSI;
+        ea.eps = c->p.eps; ea.eps2 = eps2; ea.inv_c2 = c->p.inv_c2;
+        ea.part = c->part + (size_t)(c->npad / 256 + 2) * 8;
+        ea.out = c->eout; ea.ticket = &c->tickets[2];
+        CU(launch_energy_finish(ea, s));
+    }
 
     FinishArgs fa{};
     fa.v = v; fa.m = m; fa.vsp = sp; fa.vsk = sk;
     fa.spos = c->spos; fa.acc = c->acc; fa.glob = c->glob;
     fa.nstar = nstar; fa.npad = c->npad; fa.nacc = pair_nacc(mode); fa.gsplit = k.gsplit;
-    fa.pn1 = mode == MODE_FORCE;
+    fa.pn1 = mode_has_force(mode) && c->p.inv_c2 != 0.0;
     fa.eps = c->p.eps; fa.eps2 = eps2; fa.inv_c2 = c->p.inv_c2; fa.dt = c->p.dt;
     fa.a = a_out; fa.asp = asp; fa.ask = ask;
     fa.stage = stage; fa.st = c->st; fa.ld = c->ld; fa.sums_out = sums_out;
@@ -327,6 +341,7 @@ int pn::eval_force(pn_ctx *c, const double *x, const double *v, const double *m,
     if (timed) CU(cudaEventRecord(c->ev2, s));
     c->stats.tile_j = k.tj; c->stats.i_per_thread = k.ipt; c->stats.j_split = k.js;
     c->stats.grid_split = k.gsplit; c->stats.threads = PAIR_NT;
+    c->stats.pair_variant = k.x2 ? PN_PAIR_F32X2 : PN_PAIR_SCALAR;
     c->stats.interactions = (double)nstar * (double)nstar;
     return PN_OK;
 }
@@ -423,15 +438,19 @@ extern "C" int pn_force_device(pn_ctx *c, int n, const double *d_x, const double
 // Enqueue one integration step (three evaluations with fused stage updates).
 static int step_evaluations(const pn_ctx *c) { return c->p.integrator == PN_INT_RK4 ? 4 : 3; }
 
-static int enqueue_step(pn_ctx *c, cudaStream_t s) {
+// energy_first: the first evaluation (at the step's starting state) also yields the energies of
+// that state in c->eout.
+static int enqueue_step(pn_ctx *c, cudaStream_t s, bool energy_first = false) {
     const long long ld = c->ld;
     if (c->p.integrator == PN_INT_RK4) {  // classic RK4: evaluations at y, y2, y3, y4
-        int rc = eval_force(c, c->st.x, c->st.v, c->st.m, 1, ld, nullptr, 3, 1, STAGE_RK4_1, s, false, 0);
+        int rc = eval_force(c, c->st.x, c->st.v, c->st.m, 1, ld, nullptr, 3, 1, STAGE_RK4_1, s, false, 0,
+                            nullptr, energy_first);
         for (int k = 1; k < 4 && !rc; ++k)
             rc = eval_force(c, c->st.xs, c->st.vs, c->st.m, 1, ld, nullptr, 3, 1, STAGE_RK4_1 + k, s, false, k);
         return rc;
     }
-    int rc = eval_force(c, c->st.x, c->st.v, c->st.m, 1, ld, nullptr, 3, 1, 1, s, false, 0);
+    int rc = eval_force(c, c->st.x, c->st.v, c->st.m, 1, ld, nullptr, 3, 1, 1, s, false, 0, nullptr,
+                        energy_first);
     if (!rc) rc = eval_force(c, c->st.xs, c->st.vs, c->st.m, 1, ld, nullptr, 3, 1, 2, s, false, 1);
     if (!rc) rc = eval_force(c, c->st.xs, c->st.vs, c->st.m, 1, ld, nullptr, 3, 1, 3, s, false, 2);
     return rc;
@@ -475,6 +494,34 @@ extern "C" int pn_steps(pn_ctx *c, int nsteps) {
         c->time += c->p.dt;  // Limit-sticky9.c:893
     }
     return PN_OK;
+}
+
+static int read_energy(pn_ctx *c, pn_energy_t *e) {
+    CU(cudaMemcpyAsync(c->h_eout, c->eout, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    int rc = check_device_err(c);
+    if (rc) return rc;
+    e->pot_n = c->h_eout[0];
+    e->kin_n = c->h_eout[1];
+    e->pot_pn = c->h_eout[2];
+    e->total = c->h_eout[3];
+    for (int q = 0; q < 4; ++q)
+        if (!std::isfinite(c->h_eout[q])) return set_err(PN_ERR_NONFINITE, "non-finite energy");
+    return PN_OK;
+}
+
+extern "C" int pn_steps_energy(pn_ctx *c, int nsteps, pn_energy_t *e) {
+    if (!c || !c->have_state) return set_err(PN_ERR_STATE, "pn_steps_energy: no state");
+    if (nsteps < 1 || !e) return set_err(PN_ERR_INVALID, "pn_steps_energy: nsteps, e");
+    int rc = build_step_graph(c);  // before the first launch (allocations, shapes)
+    if (rc) return rc;
+    rc = enqueue_step(c, c->stream, true);
+    if (rc) return rc;
+    c->time += c->p.dt;
+    for (int s = 1; s < nsteps; ++s) {
+        CU(cudaGraphLaunch(c->step_exec, c->stream));
+        c->time += c->p.dt;
+    }
+    return read_energy(c, e);
 }
 
 extern "C" int pn_sync(pn_ctx *c) {
@@ -570,20 +617,12 @@ static int eval_energy(pn_ctx *c, const double *x, const double *v, const double
     ea.v = v; ea.m = m; ea.sp = sp; ea.sk = sk;
     ea.spos = c->spos; ea.acc = c->acc; ea.glob = c->glob;
     ea.nstar = nstar; ea.npad = c->npad; ea.gsplit = k.gsplit;
+    ea.nacc = pair_nacc(MODE_ENERGY); ea.sphi = E_PHI; ea.spsi = E_PSI;
     ea.eps = c->p.eps; ea.eps2 = eps2; ea.inv_c2 = c->p.inv_c2;
     ea.part = c->part + (size_t)(c->npad / 256 + 2) * 8;
     ea.out = c->eout; ea.ticket = &c->tickets[2];
     CU(launch_energy_finish(ea, s));
-    CU(cudaMemcpyAsync(c->h_eout, c->eout, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
-    rc = check_device_err(c);
-    if (rc) return rc;
-    e->pot_n = c->h_eout[0];
-    e->kin_n = c->h_eout[1];
-    e->pot_pn = c->h_eout[2];
-    e->total = c->h_eout[3];
-    for (int q = 0; q < 4; ++q)
-        if (!std::isfinite(c->h_eout[q])) return set_err(PN_ERR_NONFINITE, "non-finite energy");
-    return PN_OK;
+    return read_energy(c, e);
 }
 
 extern "C" int pn_energy(pn_ctx *c, pn_energy_t *e) {

@@ -58,7 +58,8 @@ int check_device_err(pn_ctx *c);
 // One force evaluation; see pn_api.cu.  sums_out (optional) receives the per-star pair sums.
 int eval_force(pn_ctx *c, const double *x, const double *v, const double *m, long long sp,
                long long sk, double *a_out, long long asp, long long ask, int stage,
-               cudaStream_t s, bool timed, int tslot = -1, double *sums_out = nullptr);
+               cudaStream_t s, bool timed, int tslot = -1, double *sums_out = nullptr,
+               bool with_energy = false);
 void free_adjoint(pn_ctx *c);
 }  // namespace pn
 

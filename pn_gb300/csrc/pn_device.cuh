@@ -36,16 +36,19 @@ namespace pn {
 enum PairMode : int {
     MODE_NEWTON = 0,  // G only (inv_c2 == 0)
     MODE_FORCE = 1,   // G, Phi, S0, U, W
-    MODE_ENERGY = 2   // Phi, Psi
+    MODE_ENERGY = 2,  // Phi, Psi
+    MODE_FORCE_ENERGY = 3  // MODE_FORCE plus Psi: a force evaluation and the energy of its state
 };
+__host__ __device__ constexpr bool mode_has_force(int mode) { return mode == MODE_FORCE || mode == MODE_FORCE_ENERGY; }
 
 template <int MODE> struct ModeInfo;
 template <> struct ModeInfo<MODE_NEWTON> { static constexpr int NACC = 3; static constexpr int NG32 = 2; static constexpr int NG64 = 2; };
 template <> struct ModeInfo<MODE_FORCE>  { static constexpr int NACC = 9; static constexpr int NG32 = 4; static constexpr int NG64 = 6; };
 template <> struct ModeInfo<MODE_ENERGY> { static constexpr int NACC = 2; static constexpr int NG32 = 3; static constexpr int NG64 = 4; };
+template <> struct ModeInfo<MODE_FORCE_ENERGY> { static constexpr int NACC = 10; static constexpr int NG32 = 4; static constexpr int NG64 = 6; };
 
 // Accumulator slots (FP64 output arrays acc[split][slot][i]).
-enum AccSlot : int { A_GX = 0, A_GY, A_GZ, A_PHI, A_S0, A_U, A_WX, A_WY, A_WZ };
+enum AccSlot : int { A_GX = 0, A_GY, A_GZ, A_PHI, A_S0, A_U, A_WX, A_WY, A_WZ, A_PSI };
 enum AccSlotE : int { E_PHI = 0, E_PSI = 1 };
 
 // FP32 pack: NG32 float4 groups per star, group-major ([g][padded star]):
@@ -58,6 +61,19 @@ enum AccSlotE : int { E_PHI = 0, E_PSI = 1 };
 //   g0 = s.x s.y   g1 = s.z m   g2 = v.x v.y   g3 = v.z mu3   g4 = c1 c3   g5 = k35 qe
 // (s = x - x_0, the BH-relative position; qe = |s|^2 + eps^2.)
 // Padding stars (index >= nstar) have zero mass and zero weights: they add exactly 0.
+
+// Operand scalings of the packed FP32x2 sweep (pn_pair2.cuh), chosen so that constant factors
+// of the pair expressions fold into per-star pack entries and per-i registers instead of
+// costing an instruction per pair:
+//   the sweep's inverse distance is Q' = K Q: Newton's step y (1.5 - 0.5 x y^2) with both
+//   constants times K, exact in FP32 because K has a 22-bit mantissa (K ~ 1/sqrt(2), so
+//   Q'^2 ~ Q^2 / 2 carries the 1/2 of the vdj^2 term);
+//   j velocities are stored times sqrt(3), the i velocity times 4/sqrt(3) (force sweep; the
+//   cv weight 4 vdi - 3 vdj then becomes sqrt(3) (vdi* - vdj')), or times 1/sqrt(3) (energy);
+//   masses are stored as m / K^3 and mu3, k35 as mu3 / K, k35 / K; c1 as c1 - 2 |v|^2.
+// The sweep's Phi sum comes out as Phi / K^2 and is scaled back in FP64.
+constexpr double X2_K = 2965821.0 / 4194304.0;
+constexpr double X2_SQRT3 = 1.7320508075688772935;
 
 // FP64 origin of one j-tile (BH-relative), 32-byte aligned for one vector load.
 struct __align__(32) TileOrigin {
@@ -182,7 +198,7 @@ __device__ __forceinline__ void pair_accumulate(T *acc, const IState<T> &I, T jx
         acc[A_GX] = pn_fma(mQ3, dx, acc[A_GX]);
         acc[A_GY] = pn_fma(mQ3, dy, acc[A_GY]);
         acc[A_GZ] = pn_fma(mQ3, dz, acc[A_GZ]);
-    } else if constexpr (MODE == MODE_FORCE) {
+    } else if constexpr (mode_has_force(MODE)) {
         const T mQ3 = mQ * Q2;
         acc[A_GX] = pn_fma(mQ3, dx, acc[A_GX]);
         acc[A_GY] = pn_fma(mQ3, dy, acc[A_GY]);
@@ -203,6 +219,10 @@ __device__ __forceinline__ void pair_accumulate(T *acc, const IState<T> &I, T jx
         acc[A_WX] = pn_fma(cd, dx, pn_fma(cv, dvx, acc[A_WX]));
         acc[A_WY] = pn_fma(cd, dy, pn_fma(cv, dvy, acc[A_WY]));
         acc[A_WZ] = pn_fma(cd, dz, pn_fma(cv, dvz, acc[A_WZ]));
+        if constexpr (MODE == MODE_FORCE_ENERGY) {  // Psi, as MODE_ENERGY's
+            const T vivj = pn_fma(I.vz, jvz, pn_fma(I.vy, jvy, I.vx * jvx));
+            acc[A_PSI] = pn_fma(mQ, pn_fma(T(7), vivj, (vdi * vdj) * Q2), acc[A_PSI]);
+        }
     } else {  // MODE_ENERGY
         acc[E_PHI] += mQ;
         const T vivj = pn_fma(I.vz, jvz, pn_fma(I.vy, jvy, I.vx * jvx));

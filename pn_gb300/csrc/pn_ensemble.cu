@@ -230,6 +230,9 @@ static int ens_build_tables(pn_ens *e) {
         ea.nstar = nstar;
         ea.npad = e->S;
         ea.gsplit = g;
+        ea.nacc = pair_nacc(MODE_ENERGY);
+        ea.sphi = E_PHI;
+        ea.spsi = E_PSI;
         ea.eps = eps;
         ea.eps2 = eps2;
         ea.inv_c2 = e->p.inv_c2;

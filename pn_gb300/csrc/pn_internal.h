@@ -33,16 +33,17 @@ inline bool ens_shape_supported(int ipt, int js) {
 
 inline int pair_ng(bool f32, int mode) {
     if (f32) return mode == MODE_NEWTON ? ModeInfo<MODE_NEWTON>::NG32
-                  : mode == MODE_FORCE  ? ModeInfo<MODE_FORCE>::NG32
-                                        : ModeInfo<MODE_ENERGY>::NG32;
+                  : mode_has_force(mode) ? ModeInfo<MODE_FORCE>::NG32
+                                         : ModeInfo<MODE_ENERGY>::NG32;
     return mode == MODE_NEWTON ? ModeInfo<MODE_NEWTON>::NG64
-         : mode == MODE_FORCE  ? ModeInfo<MODE_FORCE>::NG64
-                               : ModeInfo<MODE_ENERGY>::NG64;
+         : mode_has_force(mode) ? ModeInfo<MODE_FORCE>::NG64
+                                : ModeInfo<MODE_ENERGY>::NG64;
 }
 
 inline int pair_nacc(int mode) {
     return mode == MODE_NEWTON ? ModeInfo<MODE_NEWTON>::NACC
          : mode == MODE_FORCE  ? ModeInfo<MODE_FORCE>::NACC
+         : mode == MODE_FORCE_ENERGY ? ModeInfo<MODE_FORCE_ENERGY>::NACC
                                : ModeInfo<MODE_ENERGY>::NACC;
 }
 

@@ -153,17 +153,18 @@ __device__ __forceinline__ void prep_body(const PrepArgs &a, int blk, int nblk) 
             pk[a.npad + j] = make_float4(lo[0], lo[1], lo[2], (float)mu3);
             pk[2 * a.npad + j] = make_float4((float)vv[0], (float)vv[1], (float)vv[2], (float)qe);
             pk[3 * a.npad + j] = make_float4((float)c1, (float)c3, (float)k35, 0.f);
-            if (a.pack2) {  // paired layout: star j is lane (j & 1) of pair j / 2
+            if (a.pack2) {  // paired layout: star j is lane (j & 1) of pair j / 2; scaled
                 const int lane = j & 1;
                 const size_t prow = (size_t)a.npad / 2;
                 float *p2 = reinterpret_cast<float *>(a.pack2 + j / 2);
+                const double K = X2_K, v2 = vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2];
                 const float vals[7][2] = {{hi[0], hi[1]},
-                                          {hi[2], (float)mj},
+                                          {hi[2], (float)(mj / (K * K * K))},
                                           {lo[0], lo[1]},
-                                          {lo[2], (float)mu3},
-                                          {(float)vv[0], (float)vv[1]},
-                                          {(float)vv[2], (float)c1},
-                                          {(float)c3, (float)k35}};
+                                          {lo[2], (float)(mu3 / K)},
+                                          {(float)(X2_SQRT3 * vv[0]), (float)(X2_SQRT3 * vv[1])},
+                                          {(float)(X2_SQRT3 * vv[2]), (float)(c1 - 2.0 * v2)},
+                                          {(float)c3, (float)(k35 / K)}};
                 for (int g = 0; g < 7; ++g) {
                     p2[g * prow * 4 + lane] = vals[g][0];
                     p2[g * prow * 4 + 2 + lane] = vals[g][1];
@@ -276,14 +277,16 @@ __device__ __forceinline__ void finish_body(const FinishArgs &a, int blk, int nb
         const double R = 1.0 / sqrt(q + eps2);
         const double R3 = R * R * R;
         const double mi = a.m[p];
+        // the force slots only (a fused-energy sweep has one more, read by the energy kernel)
+        const int nk = a.nacc < NACC_MAX ? a.nacc : NACC_MAX;
         double S[NACC_MAX];
-        for (int k = 0; k < a.nacc; ++k) {
+        for (int k = 0; k < nk; ++k) {
             double t = 0.0;
             for (int g = 0; g < a.gsplit; ++g) t += a.acc[((size_t)g * a.nacc + k) * a.npad + i];
             S[k] = t;
         }
         if (a.sums_out)
-            for (int k = 0; k < a.nacc; ++k) a.sums_out[(size_t)k * a.npad + i] = S[k];
+            for (int k = 0; k < nk; ++k) a.sums_out[(size_t)k * a.npad + i] = S[k];
         const double Gv[3] = {S[A_GX], S[A_GY], S[A_GZ]};
         double acc3[3];
         for (int k = 0; k < 3; ++k) acc3[k] = Gv[k] - m0 * R3 * s[k];  // Newton incl. BH column
@@ -382,8 +385,8 @@ __device__ __forceinline__ void energy_body(const EnergyArgs &a, int blk, int nb
         const double mi = a.m[p];
         double Phi = 0.0, Psi = 0.0;
         for (int g = 0; g < a.gsplit; ++g) {
-            Phi += a.acc[((size_t)g * 2 + E_PHI) * a.npad + i];
-            Psi += a.acc[((size_t)g * 2 + E_PSI) * a.npad + i];
+            Phi += a.acc[((size_t)g * a.nacc + a.sphi) * a.npad + i];
+            Psi += a.acc[((size_t)g * a.nacc + a.spsi) * a.npad + i];
         }
         const double q = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
         const double R = 1.0 / sqrt(q + eps2);

@@ -61,6 +61,7 @@ struct EnergyArgs {
     long long sp, sk;
     const double *spos, *acc, *glob;
     int nstar, npad, gsplit;
+    int nacc, sphi, spsi;  // pair-sum layout: slots per split and the Phi, Psi slots
     double eps, eps2, inv_c2;
     double *part, *out;  // out[4] = pot_n, kin_n, pot_pn, total
     unsigned *ticket;

@@ -4,6 +4,8 @@
 //   MODE_NEWTON  Limit-sticky9.c:36-51 (star-star part; the BH row/column is O(N))
 //   MODE_FORCE   :36-51 + the pairwise parts of :116-174 and :276-382 (see pn_device.cuh)
 //   MODE_ENERGY  the pairwise parts of :462-474 and :508-537
+//   MODE_FORCE_ENERGY  MODE_FORCE and MODE_ENERGY's Psi in one sweep (the energy of the state
+//                the force is evaluated at, Limit-sticky9.c:895-898 then :837)
 // in FP64 (T = double: parity with the reference) or mixed precision (T = float: pair terms
 // in FP32, positions relative to a per-tile FP64 origin held as FP32 hi/lo pairs, per-i
 // Kahan folding of each tile's partial sums).
@@ -107,7 +109,7 @@ __device__ __forceinline__ bool pair_block(const PairArgs &a, int ibase, int spl
                     const double2 g2 = reinterpret_cast<const double2 *>(pack)[2 * a.npad + i];
                     const double2 g3 = reinterpret_cast<const double2 *>(pack)[3 * a.npad + i];
                     I[k].vx = g2.x; I[k].vy = g2.y; I[k].vz = g3.x;
-                    if constexpr (MODE == MODE_FORCE)
+                    if constexpr (mode_has_force(MODE))
                         I[k].qe = reinterpret_cast<const double2 *>(pack)[5 * a.npad + i].y;
                 }
                 I[k].vi2 = pn_fma(I[k].vz, I[k].vz, pn_fma(I[k].vy, I[k].vy, I[k].vx * I[k].vx));
@@ -181,7 +183,7 @@ __device__ __forceinline__ bool pair_block(const PairArgs &a, int ibase, int spl
                     const float4 g2 = b[2 * tj + j];
                     jvx = g2.x; jvy = g2.y; jvz = g2.z;
                 }
-                if constexpr (MODE == MODE_FORCE) {
+                if constexpr (mode_has_force(MODE)) {
                     const float4 g3 = b[3 * tj + j];
                     jc1 = g3.x; jc3 = g3.y; jk35 = g3.z;
                 }
@@ -192,7 +194,7 @@ __device__ __forceinline__ bool pair_block(const PairArgs &a, int ibase, int spl
                     const double2 g2 = b[2 * tj + j], g3 = b[3 * tj + j];
                     jvx = g2.x; jvy = g2.y; jvz = g3.x; jmu3 = g3.y;
                 }
-                if constexpr (MODE == MODE_FORCE) {
+                if constexpr (mode_has_force(MODE)) {
                     const double2 g4 = b[4 * tj + j], g5 = b[5 * tj + j];
                     jc1 = g4.x; jc3 = g4.y; jk35 = g5.x;
                 }

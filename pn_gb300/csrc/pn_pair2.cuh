@@ -9,9 +9,17 @@
 //
 // j-data come from the "paired" pack (written by k_prep in mixed precision): for star pair k
 // of a tile, 7 float4 groups, group-major over pairs ([g][npad/2]):
-//   P0 (hx hx' hy hy')  P1 (hz hz' m m')  P2 (lx lx' ly ly')  P3 (lz lz' mu3 mu3')
-//   P4 (vx vx' vy vy')  P5 (vz vz' c1 c1')  P6 (c3 c3' k35 k35')
-// (primed = odd star), so one 128-bit shared load yields two f32x2 operands.
+//   P0 (hx hx' hy hy')  P1 (hz hz' mK mK')  P2 (lx lx' ly ly')  P3 (lz lz' mu3K mu3K')
+//   P4 (wx wx' wy wy')  P5 (wz wz' c1v c1v')  P6 (c3 c3' k35K k35K')
+// (primed = odd star), so one 128-bit shared load yields two f32x2 operands.  The entries are
+// scaled (pn_device.cuh, X2_K): mK = m / K^3, mu3K = mu3 / K, k35K = k35 / K, w = sqrt(3) v,
+// c1v = c1 - 2 |v|^2.  With the sweep's Q' = K Q these fold every constant factor of the pair
+// expressions into data: 51 FP32 operations per force pair instead of 56, and
+//   br = (rhoe - qe) c3 + c1 + |v_i|^2 - 2 |dv|^2 + 1.5 vdj^2 Q^2
+//      = (rhoe - qe) c3 + c1v + (vi* . w_j - |v_i|^2) + (w_j . d)^2 Q'^2      (vi* = 4 v_i / sqrt(3))
+//   sum_j cv dv = sum_j ct w_j - 0.75 vi* sum_j ct,  ct = mQ^3 (vi* . d - w_j . d) = cv / sqrt(3)
+// (the last term is applied once per tile).  3 K^2 = 1.5 (1 + 1.3e-7): the vdj^2 term carries
+// that relative bias, a 1PN sub-term far below the FP32 rounding of the sums.
 #pragma once
 
 #include "pn_pair.cuh"
@@ -52,17 +60,18 @@ __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
 __device__ __forceinline__ void lds2(const void *p, f2 &a, f2 &b) {
     asm volatile("ld.shared.v2.b64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "r"(smem_u32(p)));
 }
-// rsqrt of both lanes (MUFU each) refined by one Newton-Raphson step in f32x2:
-// y' = y (1.5 - 0.5 x y^2).
-__device__ __forceinline__ f2 rsqrt2(f2 x) {
+// K times the inverse square root of both lanes: MUFU rsqrt each, refined by one Newton-Raphson
+// step y' = y (1.5 - 0.5 x y^2) whose two constants are scaled by K (exact in FP32).
+__device__ __forceinline__ f2 rsqrt2k(f2 x) {
     float a, b;
     f2_unpack(x, a, b);
     float ya, yb;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(ya) : "f"(a));
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yb) : "f"(b));
     const f2 y = f2_pack(ya, yb);
-    const f2 nxh = mul2(x, f2_bcast(-0.5f));
-    const f2 r = fma2(nxh, mul2(y, y), f2_bcast(1.5f));
+    constexpr float K = (float)X2_K;
+    const f2 nxh = mul2(x, f2_bcast(-0.5f * K));
+    const f2 r = fma2(nxh, mul2(y, y), f2_bcast(1.5f * K));
     return mul2(y, r);
 }
 __device__ __forceinline__ float f2_sum(f2 v) {
@@ -72,57 +81,69 @@ __device__ __forceinline__ float f2_sum(f2 v) {
 }
 
 struct I2 {  // one i-particle, broadcast to both lanes
-    f2 ex, ey, ez, lx, ly, lz, vx, vy, vz, vi2, qe;
+    f2 ex, ey, ez, lx, ly, lz;  // hi/lo of s_i - o_tile (refreshed per tile)
+    f2 vx, vy, vz;              // force: 4 v_i / sqrt(3); energy: v_i / sqrt(3)
+    f2 nvi2, qe;                // -|v_i|^2, |s_i|^2 + eps^2
 };
+
 
 template <int MODE>
 __device__ __forceinline__ void pair2_accumulate(f2 *acc, const I2 &I, f2 jx, f2 jy, f2 jz, f2 jlx, f2 jly,
-                                                 f2 jlz, f2 jm, f2 jvx, f2 jvy, f2 jvz, f2 jmu3, f2 jc1,
+                                                 f2 jlz, f2 jm, f2 jwx, f2 jwy, f2 jwz, f2 jmu3, f2 jc1,
                                                  f2 jc3, f2 jk35, f2 eps2) {
     const f2 dx = add2(sub2(jx, I.ex), sub2(jlx, I.lx));
     const f2 dy = add2(sub2(jy, I.ey), sub2(jly, I.ly));
     const f2 dz = add2(sub2(jz, I.ez), sub2(jlz, I.lz));
     const f2 rhoe = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, eps2)));
-    const f2 Q = rsqrt2(rhoe);
-    const f2 Q2 = mul2(Q, Q);
-    const f2 mQ = mul2(jm, Q);
+    const f2 Q = rsqrt2k(rhoe);   // K Q
+    const f2 Q2 = mul2(Q, Q);     // K^2 Q^2
+    const f2 mQ = mul2(jm, Q);    // m Q / K^2
     if constexpr (MODE == MODE_NEWTON) {
-        const f2 mQ3 = mul2(mQ, Q2);
+        const f2 mQ3 = mul2(mQ, Q2);  // m Q^3
         acc[A_GX] = fma2(mQ3, dx, acc[A_GX]);
         acc[A_GY] = fma2(mQ3, dy, acc[A_GY]);
         acc[A_GZ] = fma2(mQ3, dz, acc[A_GZ]);
-    } else if constexpr (MODE == MODE_FORCE) {
+    } else if constexpr (mode_has_force(MODE)) {
+        constexpr int A_CT = ModeInfo<MODE>::NACC;  // per-tile sum of ct (folded into W per tile)
         const f2 mQ3 = mul2(mQ, Q2);
         acc[A_GX] = fma2(mQ3, dx, acc[A_GX]);
         acc[A_GY] = fma2(mQ3, dy, acc[A_GY]);
         acc[A_GZ] = fma2(mQ3, dz, acc[A_GZ]);
         acc[A_PHI] = add2(acc[A_PHI], mQ);
         acc[A_S0] = add2(acc[A_S0], mQ3);
-        const f2 uQ = mul2(jmu3, Q);
-        acc[A_U] = add2(acc[A_U], uQ);
-        const f2 dvx = sub2(jvx, I.vx), dvy = sub2(jvy, I.vy), dvz = sub2(jvz, I.vz);
-        const f2 dv2 = fma2(dvz, dvz, fma2(dvy, dvy, mul2(dvx, dvx)));
-        const f2 vdj = fma2(jvz, dz, fma2(jvy, dy, mul2(jvx, dx)));
-        const f2 vdi = fma2(I.vz, dz, fma2(I.vy, dy, mul2(I.vx, dx)));
+        acc[A_U] = add2(acc[A_U], mul2(jmu3, Q));
+        const f2 vivj = fma2(I.vz, jwz, fma2(I.vy, jwy, fma2(I.vx, jwx, I.nvi2)));  // 4 vi.vj - vi^2
+        const f2 vdj = fma2(jwz, dz, fma2(jwy, dy, mul2(jwx, dx)));                // sqrt(3) vj.d
+        const f2 vdi = fma2(I.vz, dz, fma2(I.vy, dy, mul2(I.vx, dx)));             // 4/sqrt(3) vi.d
         f2 br = fma2(sub2(rhoe, I.qe), jc3, jc1);
-        br = add2(br, fma2(f2_bcast(-2.f), dv2, I.vi2));
-        br = fma2(f2_bcast(1.5f), mul2(mul2(vdj, vdj), Q2), br);
+        br = add2(br, vivj);
+        br = fma2(mul2(vdj, vdj), Q2, br);
         const f2 cd = fma2(mQ3, br, mul2(jk35, Q));
-        const f2 cv = mul2(mQ3, fma2(f2_bcast(4.f), vdi, mul2(f2_bcast(-3.f), vdj)));
-        acc[A_WX] = fma2(cd, dx, fma2(cv, dvx, acc[A_WX]));
-        acc[A_WY] = fma2(cd, dy, fma2(cv, dvy, acc[A_WY]));
-        acc[A_WZ] = fma2(cd, dz, fma2(cv, dvz, acc[A_WZ]));
-    } else {  // MODE_ENERGY
+        const f2 ct = mul2(mQ3, sub2(vdi, vdj));
+        acc[A_WX] = fma2(cd, dx, fma2(ct, jwx, acc[A_WX]));
+        acc[A_WY] = fma2(cd, dy, fma2(ct, jwy, acc[A_WY]));
+        acc[A_WZ] = fma2(cd, dz, fma2(ct, jwz, acc[A_WZ]));
+        acc[A_CT] = add2(acc[A_CT], ct);
+        if constexpr (MODE == MODE_FORCE_ENERGY) {
+            // sum mQ' (7K^2 vivj + vdi vdj Q'^2) = 4 Psi - 7 |v_i|^2 Phi with the scaled operands
+            // above; Psi = sum/4 + 1.75 |v_i|^2 Phi is formed in FP64 when the sums are written
+            constexpr float c7 = (float)(7.0 * X2_K * X2_K);
+            acc[A_PSI] = fma2(mQ, fma2(f2_bcast(c7), vivj, mul2(mul2(vdi, vdj), Q2)), acc[A_PSI]);
+        }
+    } else {  // MODE_ENERGY: sum m Q K^2 (7 vi.vj + vdi vdj Q^2) / K^2
         acc[E_PHI] = add2(acc[E_PHI], mQ);
-        const f2 vivj = fma2(I.vz, jvz, fma2(I.vy, jvy, mul2(I.vx, jvx)));
-        const f2 vdj = fma2(jvz, dz, fma2(jvy, dy, mul2(jvx, dx)));
+        const f2 vivj = fma2(I.vz, jwz, fma2(I.vy, jwy, mul2(I.vx, jwx)));
+        const f2 vdj = fma2(jwz, dz, fma2(jwy, dy, mul2(jwx, dx)));
         const f2 vdi = fma2(I.vz, dz, fma2(I.vy, dy, mul2(I.vx, dx)));
-        acc[E_PSI] = fma2(mQ, fma2(f2_bcast(7.f), vivj, mul2(mul2(vdi, vdj), Q2)), acc[E_PSI]);
+        constexpr float c7 = (float)(7.0 * X2_K * X2_K);
+        acc[E_PSI] = fma2(mQ, fma2(f2_bcast(c7), vivj, mul2(mul2(vdi, vdj), Q2)), acc[E_PSI]);
     }
 }
 
 template <int MODE> struct Mode2 {
-    static constexpr int NG = MODE == MODE_NEWTON ? 4 : (MODE == MODE_FORCE ? 7 : 6);
+    static constexpr int NG = MODE == MODE_NEWTON ? 4 : (mode_has_force(MODE) ? 7 : 6);
+    static constexpr int NTACC = ModeInfo<MODE>::NACC + (mode_has_force(MODE) ? 1 : 0);  // + ct
+    static constexpr int PHI = mode_has_force(MODE) ? (int)A_PHI : (MODE == MODE_ENERGY ? (int)E_PHI : -1);
 };
 
 template <int MODE, int IPT>
@@ -140,6 +161,7 @@ __device__ __forceinline__ bool pair2_block(const PairArgs &a, int ibase, int sp
     constexpr int NT = PAIR_NT;
     constexpr int NG = Mode2<MODE>::NG;
     constexpr int NACC = ModeInfo<MODE>::NACC;
+    constexpr int NTACC = Mode2<MODE>::NTACC;
     const int tid = threadIdx.x;
     const int t0 = (int)(((long long)a.ntiles * split) / a.gsplit);
     const int t1 = (int)(((long long)a.ntiles * (split + 1)) / a.gsplit);
@@ -162,11 +184,12 @@ __device__ __forceinline__ bool pair2_block(const PairArgs &a, int ibase, int sp
             const float4 g = a.ipack[i];
             vx = g.x; vy = g.y; vz = g.z; qe = g.w;
         }
-        I[k].vx = f2_bcast(vx);
-        I[k].vy = f2_bcast(vy);
-        I[k].vz = f2_bcast(vz);
+        constexpr float vs = (float)(mode_has_force(MODE) ? 4.0 / X2_SQRT3 : 1.0 / X2_SQRT3);
+        I[k].vx = f2_bcast(vs * vx);
+        I[k].vy = f2_bcast(vs * vy);
+        I[k].vz = f2_bcast(vs * vz);
         I[k].qe = f2_bcast(qe);
-        I[k].vi2 = f2_bcast(fmaf(vz, vz, fmaf(vy, vy, vx * vx)));
+        I[k].nvi2 = f2_bcast(-fmaf(vz, vz, fmaf(vy, vy, vx * vx)));
     }
     float run[IPT][NACC], cmp[IPT][NACC];
 #pragma unroll
@@ -214,15 +237,15 @@ __device__ __forceinline__ bool pair2_block(const PairArgs &a, int ibase, int sp
             }
         }
         const float4 *b = buf + (size_t)stage * NG * tp;
-        f2 tacc[IPT][NACC];
+        f2 tacc[IPT][NTACC];
 #pragma unroll
         for (int k = 0; k < IPT; ++k)
 #pragma unroll
-            for (int q = 0; q < NACC; ++q) tacc[k][q] = 0ull;  // +0.0f in both lanes
+            for (int q = 0; q < NTACC; ++q) tacc[k][q] = 0ull;  // +0.0f in both lanes
 
 #pragma unroll 2
         for (int jp = 0; jp < tp; ++jp) {
-            f2 jx, jy, jz, jm, jlx, jly, jlz, jmu3, jvx = 0, jvy = 0, jvz = 0, jc1 = 0, jc3 = 0, jk35 = 0;
+            f2 jx, jy, jz, jm, jlx, jly, jlz, jmu3, jvx = 0, jvy = 0, jvz = 0, jc1 = 0, jc3 = 0, jk35 = 0;  // scaled
             lds2(b + jp, jx, jy);
             lds2(b + tp + jp, jz, jm);
             lds2(b + 2 * tp + jp, jlx, jly);
@@ -231,25 +254,48 @@ __device__ __forceinline__ bool pair2_block(const PairArgs &a, int ibase, int sp
                 lds2(b + 4 * tp + jp, jvx, jvy);
                 lds2(b + 5 * tp + jp, jvz, jc1);
             }
-            if constexpr (MODE == MODE_FORCE) lds2(b + 6 * tp + jp, jc3, jk35);
+            if constexpr (mode_has_force(MODE)) lds2(b + 6 * tp + jp, jc3, jk35);
 #pragma unroll
             for (int k = 0; k < IPT; ++k)
                 pair2_accumulate<MODE>(tacc[k], I[k], jx, jy, jz, jlx, jly, jlz, jm, jvx, jvy, jvz, jmu3, jc1,
                                        jc3, jk35, eps2);
         }
 #pragma unroll
-        for (int k = 0; k < IPT; ++k)
+        for (int k = 0; k < IPT; ++k) {
+            float ts[NACC];
 #pragma unroll
-            for (int q = 0; q < NACC; ++q) kahan_add(run[k][q], cmp[k][q], f2_sum(tacc[k][q]));
+            for (int q = 0; q < NACC; ++q) ts[q] = f2_sum(tacc[k][q]);
+            if constexpr (mode_has_force(MODE)) {  // sum ct dv = sum ct w_j - 0.75 vi* sum ct
+                const float c = -0.75f * f2_sum(tacc[k][NACC]);
+                float wx, wy, wz, u;
+                f2_unpack(I[k].vx, wx, u);
+                f2_unpack(I[k].vy, wy, u);
+                f2_unpack(I[k].vz, wz, u);
+                ts[A_WX] = fmaf(c, wx, ts[A_WX]);
+                ts[A_WY] = fmaf(c, wy, ts[A_WY]);
+                ts[A_WZ] = fmaf(c, wz, ts[A_WZ]);
+            }
+#pragma unroll
+            for (int q = 0; q < NACC; ++q) kahan_add(run[k][q], cmp[k][q], ts[q]);
+        }
         __syncthreads();
     }
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
         const int i = ibase + tid + k * NT;
-        if (i < a.nstar)
+        if (i < a.nstar) {
+            double val[NACC];
 #pragma unroll
             for (int q = 0; q < NACC; ++q)
-                a.out[((size_t)split * NACC + q) * a.npad + i] = (double)run[k][q] - (double)cmp[k][q];
+                val[q] = ((double)run[k][q] - (double)cmp[k][q]) * (q == Mode2<MODE>::PHI ? X2_K * X2_K : 1.0);
+            if constexpr (MODE == MODE_FORCE_ENERGY) {
+                float nvi2, u;
+                f2_unpack(I[k].nvi2, nvi2, u);
+                val[A_PSI] = 0.25 * val[A_PSI] - 1.75 * (double)nvi2 * val[A_PHI];
+            }
+#pragma unroll
+            for (int q = 0; q < NACC; ++q) a.out[((size_t)split * NACC + q) * a.npad + i] = val[q];
+        }
     }
     seq += (uint32_t)(t1 - t0 > 0 ? t1 - t0 : 0);
     return true;

@@ -70,8 +70,14 @@ cudaError_t launch_pair_f32(int mode, const PairCfg &c, const PairArgs &a, cudaS
             case MODE_NEWTON: return launch_two_mode<MODE_NEWTON>(c, a, s);
             case MODE_FORCE: return launch_two_mode<MODE_FORCE>(c, a, s);
             case MODE_ENERGY: return launch_two_mode<MODE_ENERGY>(c, a, s);
+            case MODE_FORCE_ENERGY: return launch_two_mode<MODE_FORCE_ENERGY>(c, a, s);
             default: return cudaErrorInvalidValue;
         }
+    }
+    if (mode == MODE_FORCE_ENERGY) {  // instantiated for the block shapes with one i-set per lane
+        PairCfg k = c;
+        if (k.js != 1 || (k.ipt != 1 && k.ipt != 2)) { k.js = 1; k.ipt = 1; }
+        return k.ipt == 2 ? launch_one<MODE_FORCE_ENERGY, 2, 1>(k, a, s) : launch_one<MODE_FORCE_ENERGY, 1, 1>(k, a, s);
     }
     switch (mode) {
         case MODE_NEWTON: return launch_mode<MODE_NEWTON>(c, a, s);

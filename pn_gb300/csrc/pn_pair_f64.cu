@@ -41,6 +41,7 @@ cudaError_t launch_pair_f64(int mode, const PairCfg &c, const PairArgs &a, cudaS
         case MODE_NEWTON: return launch_mode<MODE_NEWTON>(c, a, s);
         case MODE_FORCE: return launch_mode<MODE_FORCE>(c, a, s);
         case MODE_ENERGY: return launch_mode<MODE_ENERGY>(c, a, s);
+        case MODE_FORCE_ENERGY: return launch_mode<MODE_FORCE_ENERGY>(c, a, s);
         default: return cudaErrorInvalidValue;
     }
 }

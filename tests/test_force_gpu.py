@@ -368,3 +368,53 @@ def test_rk4_is_fourth_order(pn):
     e1 = np.abs(end(1, 1e-2, 20) - exact).max()
     e2 = np.abs(end(1, 5e-3, 40) - exact).max()
     assert 12 < e1 / e2 < 20
+
+
+# ------------------------------------------------------------------ energy fused into the force sweep
+@pytest.mark.parametrize("prec,variant,integrator,ic2", [
+    (0, 0, 0, 1.0), (0, 0, 0, 0.0), (0, 0, 1, 1.0),
+    (1, 2, 0, 1.0), (1, 1, 0, 1.0), (1, 2, 1, 1e-6),
+])
+def test_steps_energy_fused(pn, oracle, prec, variant, integrator, ic2):
+    """pn_steps_energy: the energies of the state the steps start from, taken from the first
+    force sweep (Limit-sticky9.c:896 energy() then :851 force() at the same state), equal
+    pn_energy's (FP64: 1e-12; mixed: 1e-6 of the oracle, as the separate mixed energy sweep),
+    and the steps that follow are those of pn_steps (1e-12 of the largest coordinate)."""
+    n, k = 1500, 3
+    x, v, m = random_system(n, 21, v0=0.05)
+    kw = dict(eps=0.02, dt=1e-3, inv_c2=ic2, precision=prec, pair_variant=variant, integrator=integrator)
+    with pn.Context(n, **kw) as c:
+        c.set_state(x, v, m)
+        e_sep = np.array(c.energy())
+        c.steps(k)
+        xa, va = c.get_state()
+    with pn.Context(n, **kw) as c:
+        c.set_state(x, v, m)
+        e_fused = np.array(c.steps_energy(k))
+        assert abs(c.time - k * 1e-3) < 1e-15
+        xb, vb = c.get_state()
+    if prec == 0:
+        assert np.abs(e_fused / e_sep - 1).max() <= TOL_E, (e_fused, e_sep)
+    else:
+        with pn.Context(n, eps=0.02, inv_c2=ic2) as c:
+            c.set_state(x, v, m)
+            e_ref = np.array(c.energy())
+        if ic2 == 1.0:
+            assert np.abs(e_ref / oracle.energy(x, v, m, 0.02) - 1).max() <= TOL_E
+        assert np.abs(e_fused / e_ref - 1).max() <= 1e-6, (e_fused, e_ref)
+    assert traj_err(xb, xa) <= 1e-12 and traj_err(vb, va) <= 1e-12
+
+
+def test_steps_energy_twice_and_rejects_zero_steps(pn):
+    """Back-to-back fused calls report the energy at each call's starting state."""
+    n = 700
+    x, v, m = random_system(n, 22, v0=0.05)
+    with pn.Context(n, eps=0.02, dt=1e-3) as c:
+        c.set_state(x, v, m)
+        e1 = np.array(c.steps_energy(2))
+        e_mid = np.array(c.energy())
+        e2 = np.array(c.steps_energy(1))
+        with pytest.raises(RuntimeError):
+            c.steps_energy(0)
+    assert np.abs(e2 / e_mid - 1).max() <= TOL_E
+    assert np.abs(e1 - e_mid).max() > 0  # the state moved
