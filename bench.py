@@ -59,6 +59,14 @@ def workload_config(nstars=NSTARS):
             "l2": "2x L2 overwritten before each timed step"}
 
 
+def _measured_hbm_gbs():
+    """The HBM copy bandwidth measured on this GPU type, else None."""
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return None
+
+
 def dist_init(n_gpus):
     """torchrun env -> (rank, world, torch.distributed or None)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -254,20 +262,24 @@ def run_ensemble(args):
 
 
 def run_adjoint(args):
-    """Configuration 5: N = 16384 Plummer + BH (mass fraction 0.05), 200 steps at dt = 1/1024,
-    checkpoints every 20 steps.  Loss: squared distance of the final snapshot (x, v) to a
-    target made with the BH mass x 1.1 and initial positions + N(0, 1e-3^2).  Reports the
-    adjoint's cost per step against a forward step, and checks the FP64 gradient against
-    central finite differences (h = 1e-6) on sampled coordinates and the BH mass, and the
-    mixed-precision gradient against the FP64 one."""
+    """Configuration 5: N = 16384 Plummer + BH (mass fraction 0.05), 200 steps at dt = 1/1024.
+    Loss: squared distance of the final snapshot (x, v) to a target made with the BH mass x 1.1
+    and initial positions + N(0, 1e-3^2).  Reports the cost of the adjoint per step against a
+    forward step (mixed and FP64) with checkpoints every 20 steps (segments recomputed) and with
+    every stage kept (checkpoint interval = steps, no recomputation: 1.2 GB of HBM here).
+    The FP64 gradient is checked against central differences (h = 1e-6) on sampled coordinates
+    and the BH mass over --fd-steps steps: over 200 steps at this dt the close BH passages make
+    the loss too nonlinear in the inputs for any step h to converge (h = 1e-4 .. 1e-7 disagree
+    with each other by more than 100 %), over 40 steps the differences converge to the adjoint
+    (~1e-9 at h = 1e-6).  The mixed-precision gradient is compared with the FP64 one."""
     import pn_gb300 as pn
-    ns, nsteps, K = args.adj_n, args.adj_steps, 20
+    ns, nsteps = args.adj_n, args.adj_steps
     s = pn.config_plummer(ns, 77, 0.05)
     eps = pn.plummer_eps(ns)
     rng = np.random.default_rng(5)
     n = ns + 1
 
-    def final(x, v, m, prec=0, steps=nsteps):
+    def final(x, v, m, steps, prec=0):
         with pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=prec) as c:
             c.set_state(x, v, m)
             c.steps(steps)
@@ -277,63 +289,77 @@ def run_adjoint(args):
     mt[0] *= 1.1
     xt0 = s.x + rng.normal(0, 1e-3, s.x.shape)
     xt0[0] = s.x[0]
-    xT, vT = final(xt0, s.v, mt)
 
-    def loss(x, v, m):
-        xe, ve = final(x, v, m)
-        return float(((xe - xT) ** 2).sum() + ((ve - vT) ** 2).sum())
+    def gradient(c, steps, K, xT, vT):
+        c.set_state(s.x, s.v, s.m)
+        c.adjoint_forward(steps, K)
+        xe, ve = c.get_state()
+        t0 = time.perf_counter()
+        g = c.adjoint_backward(2 * (xe - xT), 2 * (ve - vT))
+        return g, (time.perf_counter() - t0) / steps
 
-    out = {}
-    for prec in (0, 1):
+    xT, vT = final(xt0, s.v, mt, nsteps)
+    timing = {}
+    for prec in (1, 0):
         with pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=prec) as c:
             c.set_state(s.x, s.v, s.m)
             c.steps(2)  # warm-up (graph, kernels)
-            c.sync()
             c.set_state(s.x, s.v, s.m)
             t0 = time.perf_counter()
             c.steps(nsteps)
-            c.sync()
             fwd = (time.perf_counter() - t0) / nsteps
-            c.set_state(s.x, s.v, s.m)
-            c.adjoint_forward(nsteps, K)
-            xe, ve = c.get_state()
-            t0 = time.perf_counter()
-            gx, gv, gm = c.adjoint_backward(2 * (xe - xT), 2 * (ve - vT))
-            bwd = (time.perf_counter() - t0) / nsteps
-        out[prec] = dict(fwd_ms=fwd * 1e3, adj_ms=bwd * 1e3, gx=gx, gv=gv, gm=gm)
-    # central differences on sampled coordinates (FP64 forward runs)
+            r = {"fwd_ms_per_step": fwd * 1e3}
+            for K in (20, nsteps):
+                _, bwd = gradient(c, nsteps, K, xT, vT)
+                r[f"adj_ms_per_step_K{K}"] = bwd * 1e3
+                r[f"ratio_K{K}"] = bwd / fwd
+            timing["mixed" if prec else "fp64"] = r
+    # finite-difference check (FP64) over fd_steps steps
+    fs = args.fd_steps
+    xTf, vTf = final(xt0, s.v, mt, fs)
+
+    def loss(x, v, m):
+        xe, ve = final(x, v, m, fs)
+        return float(((xe - xTf) ** 2).sum() + ((ve - vTf) ** 2).sum())
+
+    grads = {}
+    for prec in (0, 1):
+        with pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=prec) as c:
+            grads[prec], _ = gradient(c, fs, 20, xTf, vTf)
+    gx, gv, gm = grads[0]
     h = 1e-6
     checks = []
-    for q in rng.choice(np.arange(3, 3 * n), args.fd_coords, replace=False):
-        p, k = divmod(int(q), 3)
-        for which in ("x", "v"):
-            a = (s.x if which == "x" else s.v).copy()
-            b = a.copy()
-            a[p, k] += h
-            b[p, k] -= h
-            lp = loss(a, s.v, s.m) if which == "x" else loss(s.x, a, s.m)
-            lm = loss(b, s.v, s.m) if which == "x" else loss(s.x, b, s.m)
-            fd = (lp - lm) / (2 * h)
-            g = out[0]["gx" if which == "x" else "gv"][p, k]
-            checks.append(abs(g - fd) / max(abs(fd), 1e-12))
+    for q in rng.choice(np.arange(3, 6 * n), args.fd_coords, replace=False):
+        which, r_ = divmod(int(q), 3 * n)
+        p_, k = divmod(r_, 3)
+        if p_ == 0:
+            continue
+        a = (s.x if which == 0 else s.v).copy()
+        b = a.copy()
+        a[p_, k] += h
+        b[p_, k] -= h
+        lp = loss(a, s.v, s.m) if which == 0 else loss(s.x, a, s.m)
+        lm = loss(b, s.v, s.m) if which == 0 else loss(s.x, b, s.m)
+        fd = (lp - lm) / (2 * h)
+        g = (gx if which == 0 else gv)[p_, k]
+        checks.append(abs(g - fd) / max(abs(fd), 1e-300))
     mp, mm = s.m.copy(), s.m.copy()
     mp[0] += h
     mm[0] -= h
     fdm = (loss(s.x, s.v, mp) - loss(s.x, s.v, mm)) / (2 * h)
-    rel_m = abs(out[0]["gm"] - fdm) / abs(fdm)
-    dmix = np.linalg.norm(out[1]["gx"] - out[0]["gx"]) / np.linalg.norm(out[0]["gx"])
-    line = {"metric": "adjoint cost per step / forward step (N=16384, 200 steps, checkpoints every 20)",
-            "value": out[1]["adj_ms"] / out[1]["fwd_ms"], "unit": "ratio", "n_gpus": 1, "steps": nsteps,
+    gx1, gv1, gm1 = grads[1]
+    dmix = np.sqrt((np.linalg.norm(gx1 - gx) ** 2 + np.linalg.norm(gv1 - gv) ** 2) /
+                   (np.linalg.norm(gx) ** 2 + np.linalg.norm(gv) ** 2))
+    line = {"metric": f"adjoint cost per step / forward step (N={ns}, {nsteps} steps, mixed)",
+            "value": timing["mixed"]["ratio_K20"], "unit": "ratio", "n_gpus": 1, "steps": nsteps,
             "warmup": 2, "higher_is_better": False, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": f"plummer_bh_N{ns}_adjoint", "bh_mass_fraction": 0.05, "dt": DT,
-                       "checkpoint_every": K, "inv_c2": INV_C2},
-            "mixed": {"fwd_ms_per_step": out[1]["fwd_ms"], "adj_ms_per_step": out[1]["adj_ms"]},
-            "fp64": {"fwd_ms_per_step": out[0]["fwd_ms"], "adj_ms_per_step": out[0]["adj_ms"],
-                     "ratio": out[0]["adj_ms"] / out[0]["fwd_ms"]},
-            "fd_check_fp64": {"coords": len(checks), "max_rel_err": float(max(checks)),
-                              "median_rel_err": float(np.median(checks)), "bh_mass_rel_err": float(rel_m)},
-            "mixed_vs_fp64_grad_rel": float(dmix),
-            "mixed_vs_fp64_dm0_rel": float(abs(out[1]["gm"] / out[0]["gm"] - 1))}
+                       "checkpoint_every": 20, "inv_c2": INV_C2},
+            "timing": timing,
+            "fd_check_fp64": {"steps": fs, "h": h, "coords": len(checks), "max_rel_err": float(max(checks)),
+                              "median_rel_err": float(np.median(checks)),
+                              "bh_mass_rel_err": float(abs(gm - fdm) / abs(fdm))},
+            "mixed_vs_fp64_grad_rel": float(dmix), "mixed_vs_fp64_dm0_rel": float(abs(gm1 / gm - 1))}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -349,16 +375,22 @@ def run_long(args, nstars, precisions, nsteps_by_prec, label):
         with pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=0) as c:
             c.set_state(s.x, s.v, s.m)
             e0 = c.energy()[3]  # energies in FP64 for both modes
-            c.set_params(precision=prec)
             k = nsteps_by_prec[prec]
+            chunks = [k // 5 + (1 if q < k % 5 else 0) for q in range(5)]
+            ms, curve, done = [], [], 0
             with ClockSampler() as clk:
-                ms = c.bench_steps(k, flush_l2=False)[0]
-            c.set_params(precision=0)
-            e1 = c.energy()[3]
+                for kc in chunks:
+                    if kc == 0:
+                        continue
+                    c.set_params(precision=prec)
+                    ms.append(c.bench_steps(kc, flush_l2=False)[0])
+                    done += kc
+                    c.set_params(precision=0)
+                    curve.append((done, float(c.energy()[3] / e0 - 1)))
+            ms = np.concatenate(ms)
             res["mixed" if prec else "fp64"] = {
                 "steps": k, "ms_per_step": float(ms.mean()), "value": 3.0 * n * n / (ms.mean() * 1e-3),
-                "energy_drift": float(e1 / e0 - 1), "drift_per_step": float((e1 / e0 - 1) / k),
-                "clocks": clk.summary()}
+                "energy_drift": curve[-1][1], "drift_curve": curve, "clocks": clk.summary()}
     line = {"metric": label, "unit": UNIT, "n_gpus": 1, "data": "synthetic",
             "config": dict(workload_config(nstars), dt=DT), **res}
     print(json.dumps(line), flush=True)
@@ -418,19 +450,25 @@ def main():
     ap.add_argument("--adjoint", action="store_true", help="configuration 5 (adjoint) instead")
     ap.add_argument("--adj-n", type=int, default=16384)
     ap.add_argument("--adj-steps", type=int, default=200)
-    ap.add_argument("--fd-coords", type=int, default=2)
+    ap.add_argument("--fd-coords", type=int, default=8)
+    ap.add_argument("--fd-steps", type=int, default=40)
     ap.add_argument("--shape", default=None, help="--profile-case launch shape: ipt,tile_j,grid_split")
     ap.add_argument("--fp64-run", type=int, default=0, metavar="STEPS",
-                    help="FP64 Plummer run at N=65536 for STEPS steps (throughput, energy drift)")
+                    help="Plummer run at N=65536, FP64 and mixed, STEPS steps each (throughput, energy drift)")
     ap.add_argument("--drift", type=int, default=0, metavar="STEPS",
-                    help="energy drift of the headline workload: mixed for STEPS, FP64 for STEPS/20")
+                    help="energy drift of the headline workload, mixed and FP64, STEPS steps each")
+    ap.add_argument("--long-mixed", type=int, default=0, metavar="STEPS",
+                    help="energy drift of the headline workload in mixed precision over STEPS steps")
     args = ap.parse_args()
     if args.fp64_run:
-        return run_long(args, 65536, (0,), {0: args.fp64_run},
-                        "FP64 integration at N=65536 (interactions/s, energy drift)")
+        return run_long(args, 65536, (0, 1), {0: args.fp64_run, 1: args.fp64_run},
+                        "integration at N=65536, FP64 and mixed (interactions/s, energy drift)")
     if args.drift:
-        return run_long(args, args.nstars, (1, 0), {1: args.drift, 0: max(1, args.drift // 20)},
+        return run_long(args, args.nstars, (1, 0), {1: args.drift, 0: args.drift},
                         "energy drift, mixed vs FP64 (interactions/s per mode)")
+    if args.long_mixed:
+        return run_long(args, args.nstars, (1,), {1: args.long_mixed},
+                        "energy drift of the mixed-precision integration (interactions/s)")
     if args.profile_case:
         return profile_case(args.profile_case, args.shape)
     if args.ensemble:
@@ -483,7 +521,7 @@ def main():
 
     # roofline of the pair sweep against the measured FP32 FMA peak
     if rank == 0:
-        flops_pair = pn.flops_per_pair(1, pn.PN_PREC_MIXED)
+        flops_pair = pn.flops_per_pair(1, pn.PN_PREC_MIXED, st.pair_variant)
         peak32 = pn.probe_fma_peak(pn.PN_PREC_MIXED)
         pairs = float(ns) * float(ns)
         achieved = pairs * flops_pair / (pair_launch_ms * 1e-3) / 1e12
@@ -495,12 +533,28 @@ def main():
                             "pair_launch_ms": pair_launch_ms,
                             "peak_source": "measured FP32 FMA throughput of this GPU (pn_probe_fma_peak)",
                             "pair_interactions_per_s": pairs / (pair_launch_ms * 1e-3)}
-        prof = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(prof):
-            try:
-                line["roofline"]["traffic"] = json.load(open(prof)).get("k_pair_force_f32_bytes_per_launch")
+        prof = os.path.join(ROOT, "profiles", "pair_sweep_traffic.json")
+        if os.path.exists(prof) and ns == NSTARS and st.pair_variant == 2:
+            try:  # DRAM bytes of one launch at this size and shape, from an ncu capture
+                pt = json.load(open(prof))
+                line["roofline"]["traffic"] = pt.get("k_pair2_force_f32_N262144_bytes_per_launch")
+                line["roofline"]["traffic_shape"] = pt.get("k_pair2_force_f32_N262144_shape")
+                line["roofline"]["ncu_fma_pipe_active_pct"] = pt.get("fma_pipe_active_pct_N65536")
             except (OSError, ValueError):
                 pass
+
+        # the O(N) kernels (k_prep + k_finish with the fused stage update) per evaluation: the
+        # step's time outside the three pair sweeps, against the measured HBM copy bandwidth
+        on_ms = max(float(step_ms.mean()) - float(pair_ms.mean()), 0.0) / 3.0
+        gs = st.grid_split
+        moved = 216 + 56 + 72 * gs + 168  # prep in/out; finish: per-star data, split sums, stage state
+        algo = 104 + 144                  # BH-star O(N) terms + one stage update, per star
+        peak_hbm = _measured_hbm_gbs()
+        line["o_n_kernels"] = {"ms_per_evaluation": on_ms, "bytes_per_star_moved": moved,
+                               "bytes_per_star_algorithmic": algo,
+                               "moved_gbs": ns * moved / (on_ms * 1e-3) / 1e9 if on_ms > 0 else None,
+                               "algorithmic_gbs": ns * algo / (on_ms * 1e-3) / 1e9 if on_ms > 0 else None,
+                               "peak_gbs": peak_hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
 
     # ---------------- e2e through the drop-in force() with host arrays
     pn.configure(pn.PN_PREC_MIXED, INV_C2)

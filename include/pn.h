@@ -168,8 +168,9 @@ void pn_autotune_clear(void);
  * launches (events captured in the step graph around each launch). */
 int pn_bench_steps(pn_ctx *ctx, int nsteps, int flush_l2, double *step_ms, double *pair_ms);
 /* Flops of one pair interaction of a sweep (mode 0 Newtonian, 1 force with 1PN, 2 energy) in
- * the given precision; an FMA counts 2, the MUFU rsqrt 1, any other add or multiply 1. */
-double pn_flops_per_pair(int mode, int precision);
+ * the given precision and pair variant (PN_PAIR_F32X2: the packed FP32x2 form, else the scalar
+ * form); an FMA counts 2, the MUFU rsqrt 1, any other add or multiply 1. */
+double pn_flops_per_pair(int mode, int precision, int pair_variant);
 /* Measured FMA throughput of this GPU (TFLOP/s, FMA = 2 flops) in FP32 (PN_PREC_MIXED) or
  * FP64 (PN_PREC_FP64): the roofline denominator of the pair sweeps. */
 int pn_probe_fma_peak(int precision, double *tflops);

@@ -28,6 +28,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libpn.so")
 PN_OK = 0
 PN_PREC_FP64 = 0
 PN_PREC_MIXED = 1
+PN_PAIR_AUTO, PN_PAIR_SCALAR, PN_PAIR_F32X2 = 0, 1, 2
 PN_NMAX = 270000
 
 _STATUS = {0: "PN_OK", -1: "PN_ERR_INVALID", -2: "PN_ERR_CUDA", -3: "PN_ERR_NOMEM",
@@ -129,7 +130,7 @@ SIGNATURES = [
     ("pn_autotune", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     ("pn_autotune_clear", None, []),
     ("pn_bench_steps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp]),
-    ("pn_flops_per_pair", ctypes.c_double, [ctypes.c_int, ctypes.c_int]),
+    ("pn_flops_per_pair", ctypes.c_double, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     ("pn_probe_fma_peak", ctypes.c_int, [ctypes.c_int, _dp]),
     ("pn_selftest_wait_timeout", ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     ("pn_device_count", ctypes.c_int, []),
@@ -509,8 +510,8 @@ def config_plummer(nstars: int, seed: int = 1, bh_fraction: float = 0.01) -> Sys
     return with_bh(xs, vs, 1.0 / nstars, bh_fraction)
 
 
-def flops_per_pair(mode: int, precision: int) -> float:
-    return lib().pn_flops_per_pair(int(mode), int(precision))
+def flops_per_pair(mode: int, precision: int, pair_variant: int = PN_PAIR_SCALAR) -> float:
+    return lib().pn_flops_per_pair(int(mode), int(precision), int(pair_variant))
 
 
 def probe_fma_peak(precision: int) -> float:

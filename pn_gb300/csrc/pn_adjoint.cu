@@ -82,11 +82,11 @@ __global__ void __launch_bounds__(256) k_finish_vjp(const FinVjpArgs a) {
     double g[NGBAR];
     for (int q = 0; q < NGBAR; ++q) g[q] = 0.0;
     if (i < a.nfill) {
-        double Gb[3] = {0, 0, 0}, Wb[3] = {0, 0, 0}, Phib = 0, S0b = 0, Ub = 0;
+        double Gb[3] = {0, 0, 0}, Wb[3] = {0, 0, 0}, Phib = 0, S0b = 0, Ub = 0, v[3] = {0, 0, 0};
         if (i < a.nstar) {
             const int p = i + 1;
             const double s[3] = {a.spos[i], a.spos[a.npad + i], a.spos[2 * a.npad + i]};
-            double v[3], ab[3], bb[3], G[3];
+            double ab[3], bb[3], G[3];
             for (int k = 0; k < 3; ++k) {
                 v[k] = a.v[p * a.vsp + k * a.vsk];
                 ab[k] = a.abar[p * a.asp + k * a.ask];
@@ -114,18 +114,26 @@ __global__ void __launch_bounds__(256) k_finish_vjp(const FinVjpArgs a) {
                 g[GB_PX + k] = gPb[k];
             }
         }
+        // |v|^2 and Wbar . v from the values the sweep itself reads (FP32 in mixed mode)
         if (a.f32) {
+            const float vf[3] = {(float)v[0], (float)v[1], (float)v[2]};
+            const float wf[3] = {(float)Wb[0], (float)Wb[1], (float)Wb[2]};
+            const float vi2 = fmaf(vf[2], vf[2], fmaf(vf[1], vf[1], vf[0] * vf[0]));
+            const float cw = fmaf(wf[2], vf[2], fmaf(wf[1], vf[1], wf[0] * vf[0]));
             float4 *ap = static_cast<float4 *>(a.apack);
             ap[i] = make_float4((float)Gb[0], (float)Gb[1], (float)Gb[2], (float)Phib);
-            ap[a.npad + i] = make_float4((float)Wb[0], (float)Wb[1], (float)Wb[2], (float)S0b);
-            ap[2 * a.npad + i] = make_float4((float)Ub, 0.f, 0.f, 0.f);
+            ap[a.npad + i] = make_float4(wf[0], wf[1], wf[2], (float)S0b);
+            ap[2 * a.npad + i] = make_float4((float)Ub, vi2, cw, 0.f);
         } else {
+            const double vi2 = fma(v[2], v[2], fma(v[1], v[1], v[0] * v[0]));
+            const double cw = fma(Wb[2], v[2], fma(Wb[1], v[1], Wb[0] * v[0]));
             double2 *ap = static_cast<double2 *>(a.apack);
             ap[i] = make_double2(Gb[0], Gb[1]);
             ap[a.npad + i] = make_double2(Gb[2], Phib);
             ap[2 * a.npad + i] = make_double2(S0b, Ub);
             ap[3 * a.npad + i] = make_double2(Wb[0], Wb[1]);
-            ap[4 * a.npad + i] = make_double2(Wb[2], 0.0);
+            ap[4 * a.npad + i] = make_double2(Wb[2], vi2);
+            ap[5 * a.npad + i] = make_double2(cw, 0.0);
         }
     }
     block_sum_n(g, NGBAR, red);
@@ -162,82 +170,127 @@ template <typename T> struct VjpState {
     T ex, ey, ez, lx, ly, lz;  // position (FP32: hi/lo relative to the tile origin)
     T vx, vy, vz, vi2, m, mu3, c1, c3, k35, qe;
     T Gx, Gy, Gz, Phi, S0, U, Wx, Wy, Wz;  // adjoint state
+    T cW;                                  // Wbar . v
 };
 
-// One (p, q) pair, both roles.  d = s_q - s_p.  Accumulates into acc[NV_VJP] of p.
+// Sums of one row p of the factored sweep.  Both roles share the two vector sums; the terms of
+// role 1 that carry a factor of row p only (Gbar_p, Wbar_p, v_p) are summed as scalars and
+// multiplied in once per row (vjp_row_out).
+enum VjpRowSum : int {
+    Y_SX = 0, Y_SY, Y_SZ, Y_VX, Y_VY, Y_VZ,
+    Y_A,    // sum mQ^3 wdv           (role 1: times -4 v_p into sbar)
+    Y_B,    // sum cd                 (role 1: times -Wbar_p into sbar)
+    Y_SG,   // sum mQ^3 wd            (role 1: times -2 v_p into vbar)
+    Y_SCV,  // sum cv                 (role 1: times -Wbar_p into vbar)
+    Y_QE,   // sum c3 mQ^3 wd         (role 1: qebar = -this)
+    Y_S0,   // sum m_q Q^3            (role 1: times -Gbar_p into sbar)
+    Y_SG2,  // sum m_p Q^3 wd'        (role 2: times -4 v_p into vbar; c1bar)
+    Y_SB2,  // sum beta'              (role 2: times v_p into sbar)
+    Y_MU3, Y_C3, Y_K35,
+    NY
+};
+
+// One (p, q) pair, both roles, d = s_q - s_p.  Role 1: p accumulates the derivative of its own
+// pair term (adjoint state of p); role 2: p is the source in q's pair term (adjoint state of q,
+// streamed with q's data).  The algebra: with F = Gbar.(mQ^3 d) + Phibar mQ + S0bar mQ^3 +
+// Ubar mu3 Q + Wbar.(cd d + cv dv) for one ordered pair (i, j),
+//   dF/dd  = mQ^3 [Gbar + 2 c3 wd d + 3 Q^2 vdj wd v_j + wdv (4 v_i - 3 v_j)] + cd Wbar - LQ Q^3 d
+//   dF/dv_i = mQ^3 wd (4 v_j - 2 v_i) + 4 mQ^3 wdv d - cv Wbar
+//   dF/dv_j = mQ^3 wd (4 (v_i - v_j) - 3 Q^2 vdj d) ... + cv Wbar   (role 2, with d -> -d)
+// LQ = 3 m Q^2 (gd + S0bar + br wd + k4 wdv) + Phibar m + Ubar mu3 + wd (3 mQ^3 vdj^2 Q + k35).
+// The self pair (q = p, d = 0) contributes only Ubar_p / eps to mu3bar; it is skipped here
+// (Q = 0) and that term is added per row, so no 1/eps^3 term has to cancel in the sums.
 template <typename T>
-__device__ __forceinline__ void vjp_pair(T *acc, const VjpState<T> &P, const VjpState<T> &Qj, T dx, T dy,
-                                         T dz, T eps2) {
+__device__ __forceinline__ void vjp_pair(T *y, const VjpState<T> &P, const VjpState<T> &Qj, T dx, T dy,
+                                         T dz, T eps2, bool self) {
     const T rhoe = pn_fma(dz, dz, pn_fma(dy, dy, pn_fma(dx, dx, eps2)));
-    const T Q = pn_rsqrt<T>(rhoe);
+    T Q = pn_rsqrt<T>(rhoe);
+    if (self) Q = T(0);
     const T Q2 = Q * Q, Q3 = Q2 * Q;
-    const T dvx = Qj.vx - P.vx, dvy = Qj.vy - P.vy, dvz = Qj.vz - P.vz;
-    const T dv2 = dvx * dvx + dvy * dvy + dvz * dvz;
-    const T vdp = P.vx * dx + P.vy * dy + P.vz * dz;   // v_p . d
-    const T vdq = Qj.vx * dx + Qj.vy * dy + Qj.vz * dz;  // v_q . d
-    // ---- p accumulates (i = p, j = q), adjoint state of p; d = s_j - s_i
-    {
-        const T mQ3 = Qj.m * Q3;
-        const T gd = P.Gx * dx + P.Gy * dy + P.Gz * dz;
-        const T wd = P.Wx * dx + P.Wy * dy + P.Wz * dz;
-        const T wdv = P.Wx * dvx + P.Wy * dvy + P.Wz * dvz;
-        const T br = Qj.c1 + Qj.c3 * (rhoe - P.qe) + P.vi2 - T(2) * dv2 + T(1.5) * vdq * vdq * Q2;
-        const T k4 = T(4) * vdp - T(3) * vdq;
-        const T cd = mQ3 * br + Qj.k35 * Q;
-        const T cv = mQ3 * k4;
-        const T LQ = T(3) * Qj.m * Q2 * (gd + P.S0 + br * wd + k4 * wdv) + P.Phi * Qj.m + P.U * Qj.mu3 +
-                     wd * (T(3) * mQ3 * vdq * vdq * Q + Qj.k35);
-        const T e2 = T(2) * Qj.c3 * wd, e3 = T(3) * Q2 * vdq * wd;
-        const T Dx = mQ3 * (P.Gx + e2 * dx + e3 * Qj.vx + wdv * (T(4) * P.vx - T(3) * Qj.vx)) + cd * P.Wx - LQ * Q3 * dx;
-        const T Dy = mQ3 * (P.Gy + e2 * dy + e3 * Qj.vy + wdv * (T(4) * P.vy - T(3) * Qj.vy)) + cd * P.Wy - LQ * Q3 * dy;
-        const T Dz = mQ3 * (P.Gz + e2 * dz + e3 * Qj.vz + wdv * (T(4) * P.vz - T(3) * Qj.vz)) + cd * P.Wz - LQ * Q3 * dz;
-        acc[V_SX] -= Dx;
-        acc[V_SY] -= Dy;
-        acc[V_SZ] -= Dz;
-        const T f4 = T(4) * mQ3 * wdv;
-        acc[V_VX] += mQ3 * wd * (T(2) * P.vx + T(4) * dvx) + f4 * dx - cv * P.Wx;
-        acc[V_VY] += mQ3 * wd * (T(2) * P.vy + T(4) * dvy) + f4 * dy - cv * P.Wy;
-        acc[V_VZ] += mQ3 * wd * (T(2) * P.vz + T(4) * dvz) + f4 * dz - cv * P.Wz;
-        acc[V_QE] -= Qj.c3 * mQ3 * wd;
+    const T vdp = pn_fma(P.vz, dz, pn_fma(P.vy, dy, P.vx * dx));     // v_p . d
+    const T vdq = pn_fma(Qj.vz, dz, pn_fma(Qj.vy, dy, Qj.vx * dx));  // v_q . d
+    const T vpq = pn_fma(P.vz, Qj.vz, pn_fma(P.vy, Qj.vy, P.vx * Qj.vx));
+    const T dv2 = pn_fma(T(-2), vpq, P.vi2 + Qj.vi2);               // |v_q - v_p|^2
+    // ---- role 1: (i, j) = (p, q), adjoint state of p
+    const T mQ3 = Qj.m * Q3;
+    const T gd = pn_fma(P.Gz, dz, pn_fma(P.Gy, dy, P.Gx * dx));
+    const T wd = pn_fma(P.Wz, dz, pn_fma(P.Wy, dy, P.Wx * dx));
+    const T wdv = pn_fma(P.Wz, Qj.vz, pn_fma(P.Wy, Qj.vy, pn_fma(P.Wx, Qj.vx, -P.cW)));
+    const T t = vdq * vdq;
+    T br = pn_fma(rhoe - P.qe, Qj.c3, Qj.c1) + pn_fma(T(-2), dv2, P.vi2);
+    br = pn_fma(T(1.5) * t, Q2, br);
+    const T k4 = pn_fma(T(4), vdp, T(-3) * vdq);
+    const T cd = pn_fma(mQ3, br, Qj.k35 * Q);
+    const T cv = mQ3 * k4;
+    T in = pn_fma(k4, wdv, pn_fma(br, wd, gd + P.S0));
+    T LQ = pn_fma(T(3) * Qj.m * Q2, in, pn_fma(Qj.m, P.Phi, P.U * Qj.mu3));
+    LQ = pn_fma(wd, pn_fma(T(3) * mQ3 * t, Q, Qj.k35), LQ);
+    const T ga = mQ3 * wd;
+    const T h = mQ3 * wdv;
+    const T al = pn_fma(T(2) * Qj.c3, ga, -LQ * Q3);
+    const T be = T(3) * pn_fma(Q2 * vdq, ga, -h);
+    y[Y_A] += h;
+    y[Y_B] += cd;
+    y[Y_SG] += ga;
+    y[Y_SCV] += cv;
+    y[Y_QE] = pn_fma(Qj.c3, ga, y[Y_QE]);
+    y[Y_S0] += mQ3;
+    // ---- role 2: (i, j) = (q, p), adjoint state of q; d' = -d, dv' = v_p - v_q
+    const T mQ3b = P.m * Q3;
+    const T gq = pn_fma(Qj.Gz, dz, pn_fma(Qj.Gy, dy, Qj.Gx * dx));  // -gd'
+    const T wq = pn_fma(Qj.Wz, dz, pn_fma(Qj.Wy, dy, Qj.Wx * dx));  // -wd'
+    const T wdv2 = pn_fma(Qj.Wz, P.vz, pn_fma(Qj.Wy, P.vy, pn_fma(Qj.Wx, P.vx, -Qj.cW)));
+    const T t2 = vdp * vdp;
+    const T rq = rhoe - Qj.qe;
+    T br2 = pn_fma(rq, P.c3, P.c1) + pn_fma(T(-2), dv2, Qj.vi2);
+    br2 = pn_fma(T(1.5) * t2, Q2, br2);
+    const T k42 = pn_fma(T(3), vdp, T(-4) * vdq);
+    const T cd2 = pn_fma(mQ3b, br2, P.k35 * Q);
+    const T cv2 = mQ3b * k42;
+    T in2 = pn_fma(k42, wdv2, pn_fma(-br2, wq, Qj.S0 - gq));
+    T LQ2 = pn_fma(T(3) * P.m * Q2, in2, pn_fma(P.m, Qj.Phi, Qj.U * P.mu3));
+    LQ2 = pn_fma(-wq, pn_fma(T(3) * mQ3b * t2, Q, P.k35), LQ2);
+    const T ga2 = -mQ3b * wq;
+    const T h2 = mQ3b * wdv2;
+    const T al2 = pn_fma(T(2) * P.c3, ga2, -LQ2 * Q3);
+    const T be2 = T(-3) * pn_fma(Q2 * vdp, ga2, h2);
+    y[Y_SG2] += ga2;
+    y[Y_SB2] += be2;
+    y[Y_MU3] = pn_fma(Qj.U, Q, y[Y_MU3]);
+    y[Y_C3] = pn_fma(ga2, rq, y[Y_C3]);
+    y[Y_K35] = pn_fma(-Q, wq, y[Y_K35]);
+    // ---- shared vector sums
+    const T cS = -(al + al2), cSv = pn_fma(T(4), h2, -be);
+    y[Y_SX] = pn_fma(cd2, Qj.Wx, pn_fma(mQ3b, Qj.Gx, pn_fma(cSv, Qj.vx, pn_fma(cS, dx, y[Y_SX]))));
+    y[Y_SY] = pn_fma(cd2, Qj.Wy, pn_fma(mQ3b, Qj.Gy, pn_fma(cSv, Qj.vy, pn_fma(cS, dy, y[Y_SY]))));
+    y[Y_SZ] = pn_fma(cd2, Qj.Wz, pn_fma(mQ3b, Qj.Gz, pn_fma(cSv, Qj.vz, pn_fma(cS, dz, y[Y_SZ]))));
+    const T cV = T(4) * (ga + ga2), cVd = pn_fma(T(4), h, -be2);
+    y[Y_VX] = pn_fma(cv2, Qj.Wx, pn_fma(cVd, dx, pn_fma(cV, Qj.vx, y[Y_VX])));
+    y[Y_VY] = pn_fma(cv2, Qj.Wy, pn_fma(cVd, dy, pn_fma(cV, Qj.vy, y[Y_VY])));
+    y[Y_VZ] = pn_fma(cv2, Qj.Wz, pn_fma(cVd, dz, pn_fma(cV, Qj.vz, y[Y_VZ])));
+}
+
+// The row's outputs (NV_VJP slots) from its sums, in FP64.  qself = 1/eps for the split whose
+// j-range holds p itself (the self pair's mu3 term), else 0.
+template <typename T>
+__device__ __forceinline__ void vjp_row_out(double *o, const double *Y, const VjpState<T> &P, double qself) {
+    const double vp[3] = {(double)P.vx, (double)P.vy, (double)P.vz};
+    const double Gp[3] = {(double)P.Gx, (double)P.Gy, (double)P.Gz};
+    const double Wp[3] = {(double)P.Wx, (double)P.Wy, (double)P.Wz};
+    for (int k = 0; k < 3; ++k) {
+        o[V_SX + k] = Y[Y_SX + k] - Gp[k] * Y[Y_S0] - 4.0 * vp[k] * Y[Y_A] - Wp[k] * Y[Y_B] + vp[k] * Y[Y_SB2];
+        o[V_VX + k] = Y[Y_VX + k] - 2.0 * vp[k] * Y[Y_SG] - Wp[k] * Y[Y_SCV] - 4.0 * vp[k] * Y[Y_SG2];
     }
-    // ---- p is the source (i = q, j = p), adjoint state of q; d' = s_p - s_q = -d
-    {
-        const T ex = -dx, ey = -dy, ez = -dz;   // d'
-        const T fx = -dvx, fy = -dvy, fz = -dvz;  // dv' = v_p - v_q
-        const T mQ3 = P.m * Q3;
-        const T gd = Qj.Gx * ex + Qj.Gy * ey + Qj.Gz * ez;
-        const T wd = Qj.Wx * ex + Qj.Wy * ey + Qj.Wz * ez;
-        const T wdv = Qj.Wx * fx + Qj.Wy * fy + Qj.Wz * fz;
-        const T vdj = -vdp, vdi = -vdq;  // v_j . d', v_i . d'
-        const T rq = rhoe - Qj.qe;
-        const T br = P.c1 + P.c3 * rq + Qj.vi2 - T(2) * dv2 + T(1.5) * vdj * vdj * Q2;
-        const T k4 = T(4) * vdi - T(3) * vdj;
-        const T cd = mQ3 * br + P.k35 * Q;
-        const T cv = mQ3 * k4;
-        const T LQ = T(3) * P.m * Q2 * (gd + Qj.S0 + br * wd + k4 * wdv) + Qj.Phi * P.m + Qj.U * P.mu3 +
-                     wd * (T(3) * mQ3 * vdj * vdj * Q + P.k35);
-        const T e2 = T(2) * P.c3 * wd, e3 = T(3) * Q2 * vdj * wd;
-        const T Dx = mQ3 * (Qj.Gx + e2 * ex + e3 * P.vx + wdv * (T(4) * Qj.vx - T(3) * P.vx)) + cd * Qj.Wx - LQ * Q3 * ex;
-        const T Dy = mQ3 * (Qj.Gy + e2 * ey + e3 * P.vy + wdv * (T(4) * Qj.vy - T(3) * P.vy)) + cd * Qj.Wy - LQ * Q3 * ey;
-        const T Dz = mQ3 * (Qj.Gz + e2 * ez + e3 * P.vz + wdv * (T(4) * Qj.vz - T(3) * P.vz)) + cd * Qj.Wz - LQ * Q3 * ez;
-        acc[V_SX] += Dx;
-        acc[V_SY] += Dy;
-        acc[V_SZ] += Dz;
-        const T g3 = T(3) * Q2 * vdj;
-        acc[V_VX] += mQ3 * wd * (T(-4) * fx + g3 * ex) - T(3) * wdv * mQ3 * ex + cv * Qj.Wx;
-        acc[V_VY] += mQ3 * wd * (T(-4) * fy + g3 * ey) - T(3) * wdv * mQ3 * ey + cv * Qj.Wy;
-        acc[V_VZ] += mQ3 * wd * (T(-4) * fz + g3 * ez) - T(3) * wdv * mQ3 * ez + cv * Qj.Wz;
-        acc[V_MU3] += Qj.U * Q;
-        const T mw = mQ3 * wd;
-        acc[V_C1] += mw;
-        acc[V_C3] += mw * rq;
-        acc[V_K35] += Q * wd;
-    }
+    o[V_QE] = -Y[Y_QE];
+    o[V_MU3] = Y[Y_MU3] + (double)P.U * qself;  // the self pair's Ubar_p mu3_p Q
+    o[V_C1] = Y[Y_SG2];
+    o[V_C3] = Y[Y_C3];
+    o[V_K35] = Y[Y_K35];
 }
 
 template <typename T> struct VjpPack;
 template <> struct VjpPack<float> { using V = float4; static constexpr int NGF = 4, NGA = 3; };
-template <> struct VjpPack<double> { using V = double2; static constexpr int NGF = 6, NGA = 5; };
+template <> struct VjpPack<double> { using V = double2; static constexpr int NGF = 6, NGA = 6; };
 
 template <typename T>
 __device__ __forceinline__ void vjp_load(VjpState<T> &S, const typename VjpPack<T>::V *f, const typename VjpPack<T>::V *ad,
@@ -251,7 +304,7 @@ __device__ __forceinline__ void vjp_load(VjpState<T> &S, const typename VjpPack<
         const float4 a0 = ad[j], a1 = ad[stride + j], a2 = ad[2 * stride + j];
         S.Gx = a0.x; S.Gy = a0.y; S.Gz = a0.z; S.Phi = a0.w;
         S.Wx = a1.x; S.Wy = a1.y; S.Wz = a1.z; S.S0 = a1.w;
-        S.U = a2.x;
+        S.U = a2.x; S.vi2 = a2.y; S.cW = a2.z;
     } else {
         const double2 g0 = f[j], g1 = f[stride + j], g2 = f[2 * stride + j], g3 = f[3 * stride + j],
                       g4 = f[4 * stride + j], g5 = f[5 * stride + j];
@@ -260,12 +313,12 @@ __device__ __forceinline__ void vjp_load(VjpState<T> &S, const typename VjpPack<
         S.vx = g2.x; S.vy = g2.y; S.vz = g3.x; S.mu3 = g3.y;
         S.c1 = g4.x; S.c3 = g4.y; S.k35 = g5.x; S.qe = g5.y;
         const double2 a0 = ad[j], a1 = ad[stride + j], a2 = ad[2 * stride + j], a3 = ad[3 * stride + j],
-                      a4 = ad[4 * stride + j];
+                      a4 = ad[4 * stride + j], a5 = ad[5 * stride + j];
         S.Gx = a0.x; S.Gy = a0.y; S.Gz = a1.x; S.Phi = a1.y;
         S.S0 = a2.x; S.U = a2.y;
-        S.Wx = a3.x; S.Wy = a3.y; S.Wz = a4.x;
+        S.Wx = a3.x; S.Wy = a3.y; S.Wz = a4.x; S.vi2 = a4.y;
+        S.cW = a5.x;
     }
-    S.vi2 = S.vx * S.vx + S.vy * S.vy + S.vz * S.vz;
 }
 
 constexpr int VJP_NT = 128;
@@ -299,8 +352,8 @@ __global__ void __launch_bounds__(VJP_NT) k_pair_vjp(const PairVjpArgs a) {
         P.ex = (T)sx; P.ey = (T)sy; P.ez = (T)sz;
         P.lx = P.ly = P.lz = T(0);
     }
-    T run[NV_VJP], cmp[NV_VJP];
-    for (int q = 0; q < NV_VJP; ++q) run[q] = cmp[q] = T(0);
+    T run[NY], cmp[NY];
+    for (int q = 0; q < NY; ++q) run[q] = cmp[q] = T(0);
     if (tid == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
@@ -339,8 +392,9 @@ __global__ void __launch_bounds__(VJP_NT) k_pair_vjp(const PairVjpArgs a) {
         }
         const V *bf = buf + (size_t)stage * NG * tj;
         const V *ba = bf + (size_t)NGF * tj;
-        T tacc[NV_VJP];
-        for (int q = 0; q < NV_VJP; ++q) tacc[q] = T(0);
+        T tacc[NY];
+        for (int q = 0; q < NY; ++q) tacc[q] = T(0);
+        const int jself = i - t * tj;  // the tile index of p itself, if this tile holds it
         for (int j = 0; j < tj; ++j) {
             VjpState<T> Qj;
             vjp_load<T>(Qj, bf, ba, tj, j);
@@ -354,15 +408,21 @@ __global__ void __launch_bounds__(VJP_NT) k_pair_vjp(const PairVjpArgs a) {
                 dy = Qj.ey - P.ey;
                 dz = Qj.ez - P.ez;
             }
-            vjp_pair<T>(F32 ? tacc : run, P, Qj, dx, dy, dz, (T)a.eps2);
+            vjp_pair<T>(F32 ? tacc : run, P, Qj, dx, dy, dz, (T)a.eps2, j == jself);
         }
         if constexpr (F32)
-            for (int q = 0; q < NV_VJP; ++q) kahan_add(run[q], cmp[q], tacc[q]);
+            for (int q = 0; q < NY; ++q) kahan_add(run[q], cmp[q], tacc[q]);
         __syncthreads();
     }
-    if (valid)
-        for (int q = 0; q < NV_VJP; ++q)
-            a.out[((size_t)split * NV_VJP + q) * a.npad + i] = F32 ? (double)run[q] - (double)cmp[q] : (double)run[q];
+    if (valid) {
+        double Y[NY], o[NV_VJP];
+        for (int q = 0; q < NY; ++q) Y[q] = F32 ? (double)run[q] - (double)cmp[q] : (double)run[q];
+        // the self-pair term belongs to one split only
+        const int tself = i / tj;
+        const bool has_self = tself >= t0 && tself < t1;
+        vjp_row_out<T>(o, Y, P, has_self ? 1.0 / sqrt(a.eps2) : 0.0);
+        for (int q = 0; q < NV_VJP; ++q) a.out[((size_t)split * NV_VJP + q) * a.npad + i] = o[q];
+    }
 }
 
 // ------------------------------------------------------------------ assembly
@@ -495,7 +555,7 @@ struct AdjointWork {
     int npad = 0;
     long long ld = 0;
     double *sums = nullptr;  // [9][npad]
-    void *apack = nullptr;   // [5][npad] x 16 B
+    void *apack = nullptr;   // [6][npad] x 16 B
     double *sdir = nullptr, *vdir = nullptr, *vjp = nullptr, *gbar = nullptr, *part = nullptr;
     int vjp_splits = 0;
     double *m0bar = nullptr;
@@ -506,6 +566,7 @@ struct AdjointWork {
     double *ckpt = nullptr;     // [nck][6][ld]  (x, v at steps 0, K, 2K, ...)
     double *seg = nullptr;      // [K][3][6][ld] evaluation states of a segment's stages
     double *segsums = nullptr;  // [K][3][9][npad]
+    int seg_holds = -1;         // segment whose stages seg/segsums hold (-1: none)
     double time0 = 0.0;
 };
 
@@ -538,7 +599,7 @@ static int adj_ensure(pn_ctx *c) {
         }
         return true;
     };
-    const bool ok = mal((void **)&w->sums, 9 * np * 8) && mal(&w->apack, 5 * np * 16) &&
+    const bool ok = mal((void **)&w->sums, 9 * np * 8) && mal(&w->apack, 6 * np * 16) &&
                     mal((void **)&w->sdir, 3 * np * 8) && mal((void **)&w->vdir, 3 * np * 8) &&
                     mal((void **)&w->gbar, 16 * 8) && mal((void **)&w->part, (np / 256 + 2) * 16 * 8) &&
                     mal((void **)&w->m0bar, 2 * 8) && mal((void **)&w->tickets, 4 * sizeof(unsigned)) &&
@@ -548,7 +609,7 @@ static int adj_ensure(pn_ctx *c) {
         return set_err(PN_ERR_NOMEM, "adjoint buffers");
     }
     CU(cudaMemset(w->tickets, 0, 4 * sizeof(unsigned)));
-    CU(cudaMemset(w->apack, 0, 5 * np * 16));
+    CU(cudaMemset(w->apack, 0, 6 * np * 16));
     CU(cudaMemset(w->work, 0, 12 * 3 * ld * 8));
     return PN_OK;
 }
@@ -610,10 +671,10 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
         qa.eps2 = eps2;
         dim3 grid((unsigned)nib, (unsigned)g);
         if (f32) {
-            const size_t smem = 128 + 2 * (size_t)(4 + 3) * tj * 16;
+            const size_t smem = 128 + 2 * (size_t)(VjpPack<float>::NGF + VjpPack<float>::NGA) * tj * 16;
             k_pair_vjp<float><<<grid, VJP_NT, smem, s>>>(qa);
         } else {
-            const size_t smem = 128 + 2 * (size_t)(6 + 5) * tj * 16;
+            const size_t smem = 128 + 2 * (size_t)(VjpPack<double>::NGF + VjpPack<double>::NGA) * tj * 16;
             k_pair_vjp<double><<<grid, VJP_NT, smem, s>>>(qa);
         }
         CU(cudaGetLastError());
@@ -667,6 +728,34 @@ extern "C" int pn_force_vjp(pn_ctx *c, const double *abar, double *xbar, double 
     return PN_OK;
 }
 
+// `steps` integration steps from the context's current state, keeping every stage's evaluation
+// state and pair sums in seg/segsums (the same evaluations as pn_steps).
+static int record_segment(pn_ctx *c, int steps) {
+    AdjointWork *w = c->adj;
+    const size_t ld = (size_t)c->ld, np = (size_t)c->npad;
+    const long long LD = c->ld;
+    cudaStream_t s = c->stream;
+    for (int t = 0; t < steps; ++t) {
+        double *S0 = w->seg + ((size_t)t * 3 + 0) * 6 * ld;
+        double *S1 = w->seg + ((size_t)t * 3 + 1) * 6 * ld;
+        double *S2 = w->seg + ((size_t)t * 3 + 2) * 6 * ld;
+        double *ss = w->segsums + (size_t)t * 3 * 9 * np;
+        CU(cudaMemcpyAsync(S0, c->st.x, 6 * ld * 8, cudaMemcpyDeviceToDevice, s));
+        int rc = eval_force(c, c->st.x, c->st.v, c->st.m, 1, LD, nullptr, 3, 1, 1, s, false, -1, ss);
+        if (rc) return rc;
+        CU(cudaMemcpyAsync(S1, c->st.xs, 3 * ld * 8, cudaMemcpyDeviceToDevice, s));
+        CU(cudaMemcpyAsync(S1 + 3 * ld, c->st.vs, 3 * ld * 8, cudaMemcpyDeviceToDevice, s));
+        rc = eval_force(c, c->st.xs, c->st.vs, c->st.m, 1, LD, nullptr, 3, 1, 2, s, false, -1, ss + 9 * np);
+        if (rc) return rc;
+        CU(cudaMemcpyAsync(S2, c->st.xs, 3 * ld * 8, cudaMemcpyDeviceToDevice, s));
+        CU(cudaMemcpyAsync(S2 + 3 * ld, c->st.vs, 3 * ld * 8, cudaMemcpyDeviceToDevice, s));
+        rc = eval_force(c, c->st.xs, c->st.vs, c->st.m, 1, LD, nullptr, 3, 1, 3, s, false, -1, ss + 18 * np);
+        if (rc) return rc;
+        c->time += c->p.dt;
+    }
+    return PN_OK;
+}
+
 extern "C" int pn_adj_forward(pn_ctx *c, int nsteps, int checkpoint_every) {
     if (!c || !c->have_state) return set_err(PN_ERR_STATE, "pn_adj_forward: no state");
     if (nsteps < 1 || checkpoint_every < 1) return set_err(PN_ERR_INVALID, "pn_adj_forward");
@@ -692,12 +781,15 @@ extern "C" int pn_adj_forward(pn_ctx *c, int nsteps, int checkpoint_every) {
         w->nck = nck;
     }
     w->time0 = c->time;
+    w->seg_holds = -1;
     for (int k = 0; k < nck; ++k) {
         CU(cudaMemcpyAsync(w->ckpt + (size_t)k * 6 * ld, c->st.x, 6 * ld * 8, cudaMemcpyDeviceToDevice, c->stream));
         const int steps = (k + 1) * K <= nsteps ? K : nsteps - k * K;
-        rc = pn_steps(c, steps);
+        // the last segment keeps its stages now, so the backward pass need not recompute it
+        rc = k == nck - 1 ? record_segment(c, steps) : pn_steps(c, steps);
         if (rc) return rc;
     }
+    w->seg_holds = nck - 1;
     return check_device_err(c);
 }
 
@@ -727,26 +819,16 @@ extern "C" int pn_adj_backward(pn_ctx *c, const double *xbar_T, const double *vb
     StageAdjArgs sa{};
     sa.Xb = Xb; sa.Vb = Vb; sa.xb = xb; sa.vb = vb; sa.x1b = x1b; sa.v1b = v1b; sa.x2b = x2b; sa.v2b = v2b;
     sa.ab = ab; sa.xF = xF; sa.vF = vF; sa.h = h; sa.n = c->n; sa.ld = LD;
+    const double time_final = c->time;
     for (int k = w->nck - 1; k >= 0; --k) {
         const int steps = (k + 1) * w->K <= w->nsteps ? w->K : w->nsteps - k * w->K;
-        // recompute the segment, keeping every stage's evaluation state and pair sums
-        CU(cudaMemcpyAsync(c->st.x, w->ckpt + (size_t)k * 6 * ld, 6 * ld * 8, cudaMemcpyDeviceToDevice, s));
-        for (int t = 0; t < steps; ++t) {
-            double *S0 = w->seg + ((size_t)t * 3 + 0) * 6 * ld;
-            double *S1 = w->seg + ((size_t)t * 3 + 1) * 6 * ld;
-            double *S2 = w->seg + ((size_t)t * 3 + 2) * 6 * ld;
-            double *ss = w->segsums + (size_t)t * 3 * 9 * np;
-            CU(cudaMemcpyAsync(S0, c->st.x, 6 * ld * 8, cudaMemcpyDeviceToDevice, s));
-            int rc = eval_force(c, c->st.x, c->st.v, c->st.m, 1, LD, nullptr, 3, 1, 1, s, false, -1, ss);
+        // recompute the segment from its checkpoint, keeping every stage's evaluation state and
+        // pair sums (the last segment's are kept by the forward pass)
+        if (w->seg_holds != k) {
+            CU(cudaMemcpyAsync(c->st.x, w->ckpt + (size_t)k * 6 * ld, 6 * ld * 8, cudaMemcpyDeviceToDevice, s));
+            int rc = record_segment(c, steps);
             if (rc) return rc;
-            CU(cudaMemcpyAsync(S1, c->st.xs, 3 * ld * 8, cudaMemcpyDeviceToDevice, s));
-            CU(cudaMemcpyAsync(S1 + 3 * ld, c->st.vs, 3 * ld * 8, cudaMemcpyDeviceToDevice, s));
-            rc = eval_force(c, c->st.xs, c->st.vs, c->st.m, 1, LD, nullptr, 3, 1, 2, s, false, -1, ss + 9 * np);
-            if (rc) return rc;
-            CU(cudaMemcpyAsync(S2, c->st.xs, 3 * ld * 8, cudaMemcpyDeviceToDevice, s));
-            CU(cudaMemcpyAsync(S2 + 3 * ld, c->st.vs, 3 * ld * 8, cudaMemcpyDeviceToDevice, s));
-            rc = eval_force(c, c->st.xs, c->st.vs, c->st.m, 1, LD, nullptr, 3, 1, 3, s, false, -1, ss + 18 * np);
-            if (rc) return rc;
+            w->seg_holds = k;
         }
         // reverse the segment's steps
         for (int t = steps - 1; t >= 0; --t) {
@@ -775,6 +857,7 @@ extern "C" int pn_adj_backward(pn_ctx *c, const double *xbar_T, const double *vb
     CU(cudaMemcpyAsync(hb.data(), Xb, 6 * ld * 8, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(m0bar, w->m0bar + 1, 8, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(c->st.x, final_state.data(), 6 * ld * 8, cudaMemcpyHostToDevice, s));
+    c->time = time_final;
     int rc = check_device_err(c);
     if (rc) return rc;
     from_soa(hb.data(), xbar_0, c->n, ld);

@@ -308,6 +308,12 @@ int pn::eval_force(pn_ctx *c, const double *x, const double *v, const double *m,
     qa.gsplit = k.gsplit; qa.eps2 = eps2;
     if (timed) CU(cudaEventRecord(c->ev0, s));
     // external event nodes, so that the events are really recorded when a captured step replays
+    // (the flag is valid only while the stream is being captured)
+    if (tslot >= 0) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        CU(cudaStreamIsCapturing(s, &cs));
+        if (cs != cudaStreamCaptureStatusActive) tslot = -1;
+    }
     if (tslot >= 0) CU(cudaEventRecordWithFlags(c->evp[2 * tslot], s, cudaEventRecordExternal));
     if (nstar > 0) {
         if (is_f32(c)) CU(launch_pair_f32(mode, k, qa, s));
@@ -843,8 +849,18 @@ extern "C" int pn_bench_steps(pn_ctx *c, int nsteps, int flush_l2, double *step_
 
 // Arithmetic work of one pair interaction in each sweep, counting an FMA as 2 flops, the MUFU
 // rsqrt as 1 and every other add/multiply as 1 (the operations written in pn_device.cuh).
-extern "C" double pn_flops_per_pair(int mode, int precision) {
+extern "C" double pn_flops_per_pair(int mode, int precision, int pair_variant) {
     const bool f32 = precision == PN_PREC_MIXED;
+    if (f32 && pair_variant == PN_PAIR_F32X2) {
+        // the packed sweep (operands pre-scaled): FORCE 51 FP32 operations of which 23 FMA,
+        // NEWTON 22 (7 FMA), ENERGY 32 (12 FMA); FMA = 2 flops, the MUFU rsqrt = 1
+        switch (mode) {
+            case MODE_NEWTON: return 30.0;
+            case MODE_FORCE: return 75.0;
+            case MODE_ENERGY: return 45.0;
+            default: return 0.0;
+        }
+    }
     switch (mode) {
         // FP32 counts include the hi/lo difference (9 vs 3) and the Newton step of the MUFU
         // rsqrt (7 vs 1 for FP64, whose rsqrt counts as one operation)

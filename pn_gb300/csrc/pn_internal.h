@@ -12,7 +12,8 @@ struct PairCfg {
     int js = 1;      // lanes sharing one i-set
     int tj = 128;    // stars per j-tile
     int gsplit = 1;  // j-range splits across CTAs
-    int x2 = 0;      // FP32 only: the packed f32x2 sweep (pn_pair2.cuh; js = 1, ipt 1 or 2)
+    int x2 = 0;      // FP32 only: the packed f32x2 sweep (pn_pair2.cuh; js = 1, ipt 1 or 2);
+                     // 2 = the same sized for 3 CTAs per SM (ipt 2, force sweeps)
 };
 
 // Launches k_pair for the given precision/mode/shape (returns cudaErrorInvalidValue for an

@@ -146,9 +146,12 @@ template <int MODE> struct Mode2 {
     static constexpr int PHI = mode_has_force(MODE) ? (int)A_PHI : (MODE == MODE_ENERGY ? (int)E_PHI : -1);
 };
 
-template <int MODE, int IPT>
+// Resident CTAs per SM the register budget is sized for: 4 at IPT = 1 (<= 128 registers); at
+// IPT = 2 either 2 (no register cap, ~196) or 3 (<= 168 registers), both offered to the tuner
+// (PairCfg::x2 = 1 or 2).
+template <int IPT, int OCC>
 constexpr int pair2_min_blocks() {
-    return IPT == 1 ? 4 : 2;
+    return IPT == 1 ? 4 : OCC;
 }
 
 // One work item of the paired sweep: the i-block at ibase (128 * IPT stars) against j-range
@@ -301,8 +304,8 @@ __device__ __forceinline__ bool pair2_block(const PairArgs &a, int ibase, int sp
     return true;
 }
 
-template <int MODE, int IPT>
-__global__ void __launch_bounds__(PAIR_NT, (pair2_min_blocks<MODE, IPT>())) k_pair2(const PairArgs a) {
+template <int MODE, int IPT, int OCC>
+__global__ void __launch_bounds__(PAIR_NT, (pair2_min_blocks<IPT, OCC>())) k_pair2(const PairArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
     float4 *buf = reinterpret_cast<float4 *>(smem + 128);

@@ -5,12 +5,12 @@
 namespace pn {
 
 // the packed f32x2 sweep (pn_pair2.cuh) on the paired pack
-template <int MODE, int IPT>
+template <int MODE, int IPT, int OCC>
 static cudaError_t launch_two(const PairCfg &c, const PairArgs &a0, cudaStream_t s) {
     PairArgs a = a0;
     a.pack = a0.pack2;
     const size_t smem = 128 + 2 * (size_t)Mode2<MODE>::NG * (size_t)(c.tj / 2) * 16;
-    auto fn = k_pair2<MODE, IPT>;
+    auto fn = k_pair2<MODE, IPT, OCC>;
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -26,8 +26,12 @@ static cudaError_t launch_two(const PairCfg &c, const PairArgs &a0, cudaStream_t
 template <int MODE>
 static cudaError_t launch_two_mode(const PairCfg &c, const PairArgs &a, cudaStream_t s) {
     if (c.js != 1 || !a.pack2 || !a.ipack) return cudaErrorInvalidValue;
-    if (c.ipt == 1) return launch_two<MODE, 1>(c, a, s);
-    if (c.ipt == 2) return launch_two<MODE, 2>(c, a, s);
+    if (c.ipt == 1) return launch_two<MODE, 1, 4>(c, a, s);
+    if (c.ipt == 2) {
+        if constexpr (mode_has_force(MODE))  // 3 CTAs per SM (x2 = 2): the force sweeps only
+            if (c.x2 == 2) return launch_two<MODE, 2, 3>(c, a, s);
+        return launch_two<MODE, 2, 2>(c, a, s);
+    }
     return cudaErrorInvalidValue;
 }
 
