@@ -136,6 +136,17 @@ int pn_energy(pn_ctx *ctx, pn_energy_t *e);
  * reference's main loop evaluates initial_energy() or energy() and then force() at the same
  * state, Limit-sticky9.c:837 or :896, then :851).  Waits for the steps, like pn_sync. */
 int pn_steps_energy(pn_ctx *ctx, int nsteps, pn_energy_t *e);
+/* pn_steps_energy in two halves: the first queues the steps and returns at once (like
+ * pn_steps), the second waits for them and returns the energies of the state they started
+ * from.  No other energy evaluation on the context may come in between. */
+int pn_steps_energy_async(pn_ctx *ctx, int nsteps);
+int pn_energy_result(pn_ctx *ctx, pn_energy_t *e);
+/* A snapshot of the current state that does not stop the GPU: pn_snapshot_begin queues a copy
+ * of x, v on the context's stream and its transfer to pinned host memory on a second stream, so
+ * steps queued after it run while the transfer goes out; pn_snapshot_end waits for the transfer
+ * only and writes host AoS x, v ([n][3]; either may be NULL).  One snapshot at a time. */
+int pn_snapshot_begin(pn_ctx *ctx);
+int pn_snapshot_end(pn_ctx *ctx, double *x, double *v);
 double pn_time(pn_ctx *ctx);
 int pn_get_stats(pn_ctx *ctx, pn_stats *s);
 /* Changes the run parameters of an existing context (e.g. precision). */

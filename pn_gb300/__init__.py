@@ -91,6 +91,10 @@ SIGNATURES = [
     ("pn_sync", ctypes.c_int, [ctypes.c_void_p]),
     ("pn_energy", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Energy)]),
     ("pn_steps_energy", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Energy)]),
+    ("pn_steps_energy_async", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    ("pn_energy_result", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Energy)]),
+    ("pn_snapshot_begin", ctypes.c_int, [ctypes.c_void_p]),
+    ("pn_snapshot_end", ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
     ("pn_time", ctypes.c_double, [ctypes.c_void_p]),
     ("pn_get_stats", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
     ("pn_set_params", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Params)]),
@@ -289,6 +293,23 @@ class Context:
         e = Energy()
         _check(lib().pn_energy(self._h, ctypes.byref(e)), "pn_energy")
         return e.as_tuple()
+
+    def steps_energy_async(self, k: int):
+        _check(lib().pn_steps_energy_async(self._h, int(k)), "pn_steps_energy_async")
+
+    def energy_result(self):
+        e = Energy()
+        _check(lib().pn_energy_result(self._h, ctypes.byref(e)), "pn_energy_result")
+        return e.as_tuple()
+
+    def snapshot_begin(self):
+        _check(lib().pn_snapshot_begin(self._h), "pn_snapshot_begin")
+
+    def snapshot_end(self):
+        x = np.zeros((self.n, 3))
+        v = np.zeros((self.n, 3))
+        _check(lib().pn_snapshot_end(self._h, _p(x), _p(v)), "pn_snapshot_end")
+        return x, v
 
     def steps_energy(self, k: int):
         """Energies of the current state (as energy()) from the first force sweep of the next

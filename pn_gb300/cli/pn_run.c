@@ -99,11 +99,13 @@ int main(int argc, char **argv) {
     }
     /* An energy owed for the current state (initial_energy at :837, or energy at a snapshot,
      * :896) is taken from the force sweep that starts the next steps at that same state
-     * (pn_steps_energy) and printed when those steps are done; printed lines and their order
-     * are the reference's.  A run that ends on a snapshot, or that writes checkpoints, uses a
-     * separate energy sweep. */
+     * (pn_steps_energy_async) and printed when those steps are done; a snapshot's state is
+     * copied out while those steps run (pn_snapshot_begin/end) and written to the file before
+     * the energy line is printed.  Printed lines and their order are the reference's.  A run
+     * that ends on a snapshot, or that writes checkpoints, uses a separate energy sweep. */
     enum { OWE_NONE, OWE_INITIAL, OWE_SNAPSHOT } owed = resume ? OWE_NONE : OWE_INITIAL;
     double owed_time = 0.0;
+    int snap_pending = 0;
     if (owed == OWE_INITIAL && !(time < endtime)) {
         rc = pn_energy(ctx, &e);
         if (rc) return die("pn_energy", rc);
@@ -121,8 +123,16 @@ int main(int argc, char **argv) {
             k++;
             if (t >= eouttime) break;
         }
+        rc = owed != OWE_NONE ? pn_steps_energy_async(ctx, k) : pn_steps(ctx, k);
+        if (rc) return die("pn_steps", rc);
+        if (snap_pending) {  /* the previous snapshot, written while these steps run */
+            rc = pn_snapshot_end(ctx, x, v);
+            if (!rc) rc = write_snap(output, n, x, v, lossless);
+            if (rc) return die("snapshot", rc);
+            snap_pending = 0;
+        }
         if (owed != OWE_NONE) {
-            rc = pn_steps_energy(ctx, k, &e);
+            rc = pn_energy_result(ctx, &e);
             if (rc) return die("pn_steps_energy", rc);
             if (owed == OWE_INITIAL) {
                 print_energy(0.0, &e, 0, 0.0);
@@ -132,17 +142,16 @@ int main(int argc, char **argv) {
             }
             owed = OWE_NONE;
         } else {
-            rc = pn_steps(ctx, k);
-            if (!rc) rc = pn_sync(ctx);
+            rc = pn_sync(ctx);
             if (rc) return die("pn_steps", rc);
         }
         time = t;
         if (time >= eouttime) {                               /* :895-906 */
             eouttime += deouttime;
-            rc = pn_get_state(ctx, x, v);
-            if (!rc) rc = write_snap(output, n, x, v, lossless);
-            if (rc) return die("snapshot", rc);
             if (ckpt || !(time < endtime)) {
+                rc = pn_get_state(ctx, x, v);
+                if (!rc) rc = write_snap(output, n, x, v, lossless);
+                if (rc) return die("snapshot", rc);
                 rc = pn_energy(ctx, &e);
                 if (rc) return die("pn_energy", rc);
                 print_energy(time, &e, 1, init_ene);
@@ -151,6 +160,9 @@ int main(int argc, char **argv) {
                     if (rc) return die("checkpoint", rc);
                 }
             } else {
+                rc = pn_snapshot_begin(ctx);
+                if (rc) return die("snapshot", rc);
+                snap_pending = 1;
                 owed = OWE_SNAPSHOT;
                 owed_time = time;
             }

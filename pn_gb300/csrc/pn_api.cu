@@ -180,6 +180,12 @@ static void free_ctx(pn_ctx *c) {
     for (cudaEvent_t e : c->evp)
         if (e) cudaEventDestroy(e);
     if (c->flush) cudaFree(c->flush);
+    if (c->snap_stream) cudaStreamSynchronize(c->snap_stream);
+    if (c->snap_dev) cudaFree(c->snap_dev);
+    if (c->snap_host) cudaFreeHost(c->snap_host);
+    if (c->snap_taken) cudaEventDestroy(c->snap_taken);
+    if (c->snap_done) cudaEventDestroy(c->snap_done);
+    if (c->snap_stream) cudaStreamDestroy(c->snap_stream);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -515,9 +521,9 @@ static int read_energy(pn_ctx *c, pn_energy_t *e) {
     return PN_OK;
 }
 
-extern "C" int pn_steps_energy(pn_ctx *c, int nsteps, pn_energy_t *e) {
+extern "C" int pn_steps_energy_async(pn_ctx *c, int nsteps) {
     if (!c || !c->have_state) return set_err(PN_ERR_STATE, "pn_steps_energy: no state");
-    if (nsteps < 1 || !e) return set_err(PN_ERR_INVALID, "pn_steps_energy: nsteps, e");
+    if (nsteps < 1) return set_err(PN_ERR_INVALID, "pn_steps_energy: nsteps");
     int rc = build_step_graph(c);  // before the first launch (allocations, shapes)
     if (rc) return rc;
     rc = enqueue_step(c, c->stream, true);
@@ -527,7 +533,57 @@ extern "C" int pn_steps_energy(pn_ctx *c, int nsteps, pn_energy_t *e) {
         CU(cudaGraphLaunch(c->step_exec, c->stream));
         c->time += c->p.dt;
     }
+    return PN_OK;
+}
+
+extern "C" int pn_energy_result(pn_ctx *c, pn_energy_t *e) {
+    if (!c || !e) return set_err(PN_ERR_INVALID, "pn_energy_result");
     return read_energy(c, e);
+}
+
+extern "C" int pn_steps_energy(pn_ctx *c, int nsteps, pn_energy_t *e) {
+    if (!e) return set_err(PN_ERR_INVALID, "pn_steps_energy: e");
+    int rc = pn_steps_energy_async(c, nsteps);
+    return rc ? rc : read_energy(c, e);
+}
+
+// ------------------------------------------------------------------ asynchronous snapshots
+extern "C" int pn_snapshot_begin(pn_ctx *c) {
+    if (!c || !c->have_state) return set_err(PN_ERR_STATE, "pn_snapshot_begin: no state");
+    if (c->snap_pending) return set_err(PN_ERR_STATE, "pn_snapshot_begin: previous snapshot not ended");
+    const size_t bytes = 6 * (size_t)c->ld * sizeof(double);  // x and v are adjacent in the state
+    if (!c->snap_dev) {
+        if (cudaMalloc(&c->snap_dev, bytes) != cudaSuccess || cudaMallocHost(&c->snap_host, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(PN_ERR_NOMEM, "snapshot buffers");
+        }
+        CU(cudaStreamCreateWithFlags(&c->snap_stream, cudaStreamNonBlocking));
+        CU(cudaEventCreateWithFlags(&c->snap_taken, cudaEventDisableTiming));
+        CU(cudaEventCreateWithFlags(&c->snap_done, cudaEventDisableTiming));
+    }
+    // the device copy is ordered on the context's stream (before any later step); the transfer
+    // to the host runs on the copy stream, concurrently with those steps
+    CU(cudaMemcpyAsync(c->snap_dev, c->st.x, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaEventRecord(c->snap_taken, c->stream));
+    CU(cudaStreamWaitEvent(c->snap_stream, c->snap_taken, 0));
+    CU(cudaMemcpyAsync(c->snap_host, c->snap_dev, bytes, cudaMemcpyDeviceToHost, c->snap_stream));
+    CU(cudaEventRecord(c->snap_done, c->snap_stream));
+    c->snap_pending = true;
+    c->snap_n = c->n;
+    return PN_OK;
+}
+
+extern "C" int pn_snapshot_end(pn_ctx *c, double *x, double *v) {
+    if (!c || !c->snap_pending) return set_err(PN_ERR_STATE, "pn_snapshot_end: no snapshot begun");
+    c->snap_pending = false;
+    CU(cudaEventSynchronize(c->snap_done));
+    const size_t ld = (size_t)c->ld;
+    for (int p = 0; p < c->snap_n; ++p)
+        for (int k = 0; k < 3; ++k) {
+            if (x) x[3 * p + k] = c->snap_host[k * ld + p];
+            if (v) v[3 * p + k] = c->snap_host[3 * ld + k * ld + p];
+        }
+    return set_err(PN_OK, nullptr);
 }
 
 extern "C" int pn_sync(pn_ctx *c) {

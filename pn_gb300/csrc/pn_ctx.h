@@ -45,6 +45,13 @@ struct pn_ctx {
     pn::PairCfg cfg_force{}, cfg_energy{};
     bool cfg_set = false;
     AdjointWork *adj = nullptr;  // buffers of the adjoint (created on first use)
+    // asynchronous snapshots (created on first use): device copy of x, v, its pinned host image,
+    // the copy stream and the events ordering them against the context's stream
+    double *snap_dev = nullptr, *snap_host = nullptr;
+    cudaStream_t snap_stream = nullptr;
+    cudaEvent_t snap_taken = nullptr, snap_done = nullptr;
+    bool snap_pending = false;
+    int snap_n = 0;
 };
 
 namespace pn {

@@ -420,3 +420,28 @@ def test_steps_energy_twice_and_rejects_zero_steps(pn):
             c.steps_energy(0)
     assert np.abs(e2 / e_mid - 1).max() <= TOL_E
     assert np.abs(e1 - e_mid).max() > 0  # the state moved
+
+
+def test_snapshot_async_is_the_state_it_was_taken_at(pn):
+    """pn_snapshot_begin/end: the state at the call, while later steps already run."""
+    n = 900
+    x, v, m = random_system(n, 23, v0=0.05)
+    with pn.Context(n, eps=0.02, dt=1e-3) as c:
+        c.set_state(x, v, m)
+        c.steps(2)
+        x2, v2 = c.get_state()
+        c.snapshot_begin()
+        c.steps_energy_async(3)
+        xs, vs = c.snapshot_end()
+        e = np.array(c.energy_result())
+        with pytest.raises(RuntimeError):
+            c.snapshot_end()
+        x5, _ = c.get_state()
+        e2 = np.array(c.energy())
+    assert np.array_equal(xs, x2) and np.array_equal(vs, v2)
+    assert not np.array_equal(x5, x2)
+    with pn.Context(n, eps=0.02, dt=1e-3) as c:
+        c.set_state(x2, v2, m)
+        e_ref = np.array(c.energy())
+    assert np.abs(e - e_ref).max() <= TOL_E * np.abs(e_ref).max()
+    assert np.abs(e2 - e_ref).max() > 0
