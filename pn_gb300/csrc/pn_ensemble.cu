@@ -69,6 +69,7 @@ struct pn_ens {
     int P = 0, S = 0, LD = 0, B = 0;  // particles, star slots, state leading dim, 256-blocks
     pn_params p{};
     int ipt = 2, js = 1;
+    int x2 = 0;  // mixed precision: the packed FP32x2 sweep (js = 1)
     ClassShape cls[32];
     cudaStream_t stream = nullptr;
     double *state = nullptr;
@@ -78,6 +79,7 @@ struct pn_ens {
            *eout = nullptr;
     int acc_splits = 0;
     void *pack = nullptr;
+    float4 *pack2 = nullptr, *ipack = nullptr;  // mixed precision: paired pack [7][S/2], i-data [S]
     TileOrigin *torg = nullptr;
     unsigned *tickets = nullptr, *counter = nullptr;
     int *err = nullptr;
@@ -101,7 +103,7 @@ static void ens_free(pn_ens *e) {
     if (!e) return;
     if (e->step_exec) cudaGraphExecDestroy(e->step_exec);
     void *bufs[] = {e->state, e->a_aos, e->spos, e->acc, e->ppart, e->fpart, e->glob, e->eout,
-                    e->pack, e->torg, e->tickets, e->counter, e->err, e->blockmap, e->items,
+                    e->pack, e->pack2, e->ipack, e->torg, e->tickets, e->counter, e->err, e->blockmap, e->items,
                     e->t_prep, e->t_fin, e->t_en, e->t_pair};
     for (void *b : bufs)
         if (b) cudaFree(b);
@@ -167,6 +169,10 @@ static int ens_build_tables(pn_ens *e) {
             pa.f32 = f32;
             pa.eps2 = eps2;
             pa.pack = static_cast<char *>(e->pack) + so * 16;
+            if (e->pack2) {  // slot offsets are multiples of 256, so so / 2 is a whole pair row
+                pa.pack2 = e->pack2 + so / 2;
+                pa.ipack = e->ipack + so;
+            }
             pa.torg = e->torg + so / 32;  // tile origins at 32-slot granularity (tj >= 32)
             pa.spos = e->spos + so;
             pa.part = e->ppart + (size_t)e->blk0[c] * NGLOB;
@@ -177,6 +183,10 @@ static int ens_build_tables(pn_ens *e) {
             PairArgs &qa = tq[pm * nc + c];
             qa = PairArgs{};
             qa.pack = static_cast<char *>(e->pack) + so * 16;
+            if (e->pack2) {
+                qa.pack2 = e->pack2 + so / 2;
+                qa.ipack = e->ipack + so;
+            }
             qa.torg = e->torg + so / 32;
             qa.spos = e->spos + so;
             qa.out = e->acc + so;
@@ -275,10 +285,14 @@ static int ens_tjmax(const pn_ens *e) {
 
 static int ens_pair_launch(pn_ens *e, int mode, const PairArgs *tab, cudaStream_t s) {
     ECU(cudaMemsetAsync(e->counter, 0, sizeof(unsigned), s));
-    cudaError_t r = ens_f32(e) ? launch_pair_ens_f32(mode, e->ipt, e->js, ens_tjmax(e), 0, tab,
-                                                    e->items, e->nitems, e->counter, s)
-                               : launch_pair_ens_f64(mode, e->ipt, e->js, ens_tjmax(e), 0, tab,
-                                                    e->items, e->nitems, e->counter, s);
+    cudaError_t r;
+    if (ens_f32(e) && e->x2 && e->js == 1 && e->pack2)
+        r = launch_pair2_ens_f32(mode, e->ipt, ens_tjmax(e), 0, tab, e->items, e->nitems, e->counter, s);
+    else
+        r = ens_f32(e) ? launch_pair_ens_f32(mode, e->ipt, e->js, ens_tjmax(e), 0, tab,
+                                             e->items, e->nitems, e->counter, s)
+                       : launch_pair_ens_f64(mode, e->ipt, e->js, ens_tjmax(e), 0, tab,
+                                             e->items, e->nitems, e->counter, s);
     if (r != cudaSuccess) return fail(PN_ERR_CUDA, "pair_ens", r);
     return PN_OK;
 }
@@ -339,7 +353,7 @@ extern "C" int pn_ens_create(pn_ens **out, int nclusters, const int *n, const do
     e->S = S;
     e->B = B;
     e->LD = (int)rup(P, 256);
-    if (ens_f32(e)) { e->ipt = 2; e->js = 1; } else { e->ipt = 1; e->js = 4; }
+    if (ens_f32(e)) { e->ipt = 2; e->js = 1; e->x2 = 1; } else { e->ipt = 1; e->js = 4; }
     for (int k = 0; k < 32; ++k) {
         e->cls[k].tj = ens_f32(e) ? (k >= 12 ? 256 : 128) : 128;
         e->cls[k].tiles_per_item = 32;
@@ -358,6 +372,11 @@ extern "C" int pn_ens_create(pn_ens **out, int nclusters, const int *n, const do
     if (cudaMalloc(&e->a_aos, 3 * ld * sizeof(double))) return bad("a");
     if (cudaMalloc(&e->spos, 3 * (size_t)S * sizeof(double))) return bad("spos");
     if (cudaMalloc(&e->pack, 6 * (size_t)S * 16)) return bad("pack");
+    if (ens_f32(e)) {
+        if (cudaMalloc(&e->pack2, 7 * ((size_t)S / 2) * 16) || cudaMalloc(&e->ipack, (size_t)S * 16) ||
+            cudaMemset(e->pack2, 0, 7 * ((size_t)S / 2) * 16) || cudaMemset(e->ipack, 0, (size_t)S * 16))
+            return bad("pack2");
+    }
     if (cudaMalloc(&e->torg, ((size_t)S / 32 + 1) * sizeof(TileOrigin))) return bad("torg");
     if (cudaMalloc(&e->ppart, (size_t)B * NGLOB * sizeof(double))) return bad("ppart");
     if (cudaMalloc(&e->fpart, (size_t)B * 8 * sizeof(double))) return bad("fpart");
@@ -515,6 +534,7 @@ extern "C" int pn_ens_set_shape(pn_ens *e, int ipt, int js, int size_class_, int
         if (!ens_shape_supported(ipt, js)) return fail(PN_ERR_INVALID, "shape");
         e->ipt = ipt;
         e->js = js;
+        e->x2 = 0;  // an explicit shape selects the scalar sweep
     }
     if (size_class_ >= 0) {
         if (size_class_ > 31 || (tile_j != 32 && tile_j != 64 && tile_j != 128 && tile_j != 256) ||
@@ -582,13 +602,15 @@ extern "C" int pn_ens_autotune(pn_ens *e) {
             }
         e->cls[k] = best;
     }
-    // launch-wide (ipt, js)
-    const int shapes[3][2] = {{1, 1}, {2, 1}, {1, 4}};
-    int bi = e->ipt, bj = e->js;
+    // launch-wide (ipt, js, packed)
+    const int shapes[5][3] = {{1, 1, 0}, {2, 1, 0}, {1, 4, 0}, {1, 1, 1}, {2, 1, 1}};
+    int bi = e->ipt, bj = e->js, bx = e->x2;
     float best_ms = 1e30f;
     for (auto &sh : shapes) {
+        if (sh[2] && !(f32 && e->pack2)) continue;
         e->ipt = sh[0];
         e->js = sh[1];
+        e->x2 = sh[2];
         int rc = ens_build_tables(e);
         if (rc) return rc;
         float ms = 0.f, ms2 = 0.f;
@@ -600,10 +622,12 @@ extern "C" int pn_ens_autotune(pn_ens *e) {
             best_ms = ms;
             bi = sh[0];
             bj = sh[1];
+            bx = sh[2];
         }
     }
     e->ipt = bi;
     e->js = bj;
+    e->x2 = bx;
     int rc = ens_build_tables(e);
     if (rc) return rc;
     return ens_check(e);

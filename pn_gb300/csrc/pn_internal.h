@@ -28,6 +28,9 @@ cudaError_t launch_pair_ens_f32(int mode, int ipt, int js, int tjmax, int grid, 
                                 const int4 *items, int nitems, unsigned *counter, cudaStream_t s);
 cudaError_t launch_pair_ens_f64(int mode, int ipt, int js, int tjmax, int grid, const PairArgs *tab,
                                 const int4 *items, int nitems, unsigned *counter, cudaStream_t s);
+// the packed FP32x2 form of the ensemble sweep (tab[c].pack2 / ipack set; js = 1, ipt 1 or 2)
+cudaError_t launch_pair2_ens_f32(int mode, int ipt, int tjmax, int grid, const PairArgs *tab,
+                                 const int4 *items, int nitems, unsigned *counter, cudaStream_t s);
 inline bool ens_shape_supported(int ipt, int js) {
     return (js == 1 && (ipt == 1 || ipt == 2)) || (ipt == 1 && js == 4);
 }

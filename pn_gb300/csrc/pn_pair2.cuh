@@ -319,4 +319,34 @@ __global__ void __launch_bounds__(PAIR_NT, (pair2_min_blocks<IPT, OCC>())) k_pai
     pair2_block<MODE, IPT>(a, blockIdx.x * (PAIR_NT * IPT), blockIdx.y, bars, buf, seq);
 }
 
+// Ensemble form: one persistent launch over the work items of every cluster, as k_pair_ens
+// (pn_pair.cuh), each item swept in the packed form on its cluster's paired pack (the table's
+// pack2).  The counter only grows, so every CTA leaves after at most nitems + 1 fetches.
+template <int MODE, int IPT>
+__global__ void __launch_bounds__(PAIR_NT, (pair2_min_blocks<IPT, 2>()))
+    k_pair2_ens(const PairArgs *tab, const int4 *items, int nitems, unsigned *counter) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    float4 *buf = reinterpret_cast<float4 *>(smem + 128);
+    __shared__ int cur;
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t seq = 0;
+    for (;;) {
+        if (threadIdx.x == 0) cur = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int w = cur;
+        __syncthreads();  // everyone has read cur before thread 0 fetches the next item
+        if (w >= nitems) break;
+        const int4 it = items[w];
+        PairArgs a = tab[it.x];
+        a.pack = a.pack2;
+        if (!pair2_block<MODE, IPT>(a, it.y, it.z, bars, buf, seq)) break;
+    }
+}
+
 }  // namespace pn

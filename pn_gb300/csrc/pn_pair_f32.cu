@@ -131,6 +131,47 @@ static cudaError_t launch_ens_mode(int ipt, int js, int tjmax, int grid, const P
     return cudaErrorInvalidValue;
 }
 
+template <int MODE, int IPT>
+static cudaError_t launch_ens_two(int tjmax, int grid, const PairArgs *tab, const int4 *items, int nitems,
+                                  unsigned *counter, cudaStream_t s) {
+    const size_t smem = 128 + 2 * (size_t)Mode2<MODE>::NG * (size_t)(tjmax / 2) * 16;
+    auto fn = k_pair2_ens<MODE, IPT>;
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    if (grid <= 0) {  // persistent: as many CTAs as fit on the GPU at once
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, PAIR_NT, smem);
+        grid = sms * (per > 0 ? per : 1);
+    }
+    fn<<<grid, PAIR_NT, smem, s>>>(tab, items, nitems, counter);
+    return cudaGetLastError();
+}
+
+template <int MODE>
+static cudaError_t launch_ens_two_mode(int ipt, int tjmax, int grid, const PairArgs *tab, const int4 *items,
+                                       int nitems, unsigned *counter, cudaStream_t s) {
+    if (ipt == 1) return launch_ens_two<MODE, 1>(tjmax, grid, tab, items, nitems, counter, s);
+    if (ipt == 2) return launch_ens_two<MODE, 2>(tjmax, grid, tab, items, nitems, counter, s);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_pair2_ens_f32(int mode, int ipt, int tjmax, int grid, const PairArgs *tab,
+                                 const int4 *items, int nitems, unsigned *counter, cudaStream_t s) {
+    if (nitems <= 0) return cudaSuccess;
+    switch (mode) {
+        case MODE_NEWTON: return launch_ens_two_mode<MODE_NEWTON>(ipt, tjmax, grid, tab, items, nitems, counter, s);
+        case MODE_FORCE: return launch_ens_two_mode<MODE_FORCE>(ipt, tjmax, grid, tab, items, nitems, counter, s);
+        case MODE_ENERGY: return launch_ens_two_mode<MODE_ENERGY>(ipt, tjmax, grid, tab, items, nitems, counter, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t launch_pair_ens_f32(int mode, int ipt, int js, int tjmax, int grid, const PairArgs *tab,
                                  const int4 *items, int nitems, unsigned *counter, cudaStream_t s) {
     if (nitems <= 0) return cudaSuccess;
