@@ -59,12 +59,15 @@ def test_force_vjp_directional_fd(pn, oracle, n, ic2):
     assert abs(m0b - want) <= 1e-6 * (abs(want) + 1e-9), (m0b, want)
 
 
-def test_force_vjp_mixed_close_to_fp64(pn):
-    x, v, m = system(2000, 3)
+@pytest.mark.parametrize("n", [2000, 2, 130, 257, 385])
+def test_force_vjp_mixed_close_to_fp64(pn, n):
+    """The mixed-precision VJP (packed sweep, two rows per thread, ragged last block) against
+    the FP64 one: 1e-5 RMS relative."""
+    x, v, m = system(n, 3)
     abar = np.random.default_rng(2).normal(size=x.shape)
     out = []
     for prec in (0, 1):
-        with pn.Context(2000, eps=0.02, precision=prec) as c:
+        with pn.Context(n, eps=0.02, precision=prec) as c:
             c.set_state(x, v, m)
             out.append(c.force_vjp(abar))
     for k in (0, 1):
