@@ -7,8 +7,7 @@
 //                     (generated from the same formulas, pn_finish_vjp_gen.cuh): adjoints of
 //                     the star's pair sums (the "adjoint state" Gbar, Phibar, S0bar, Ubar, Wbar),
 //                     of its own s, v, of the global sums and of m0
-//   k_pair_vjp        (O(N^2)) one symmetric sweep (mixed precision: k_pair_vjp2 on packed
-//                     FP32x2 instructions, two rows per thread): for star p against every star q, the pair
+//   k_pair_vjp        (O(N^2)) one symmetric sweep: for star p against every star q, the pair
 //                     term's derivative with p as the accumulating particle (adjoint state of p)
 //                     and with p as the source particle (adjoint state of q streamed with q's
 //                     data), i.e. the pairwise tidal-tensor contraction with the adjoint state
@@ -30,7 +29,6 @@
 
 #include "pn_ctx.h"
 #include "pn_finish_vjp_gen.cuh"
-#include "pn_vjp2.cuh"
 
 using namespace pn;
 
@@ -203,15 +201,11 @@ enum VjpRowSum : int {
 // The self pair (q = p, d = 0) contributes only Ubar_p / eps to mu3bar; it is skipped here
 // (Q = 0) and that term is added per row, so no 1/eps^3 term has to cancel in the sums.
 template <typename T>
-__device__ __forceinline__ T vjp_self_mask(T Q, bool self) { return self ? T(0) : Q; }
-
-// T = float / double (one pair), or V2 (two rows per thread, pn_vjp2.cuh); self: the pair is
-// the row's own star (bool, or a per-lane keep mask of 1 / 0 for V2).
-template <typename T, typename S>
 __device__ __forceinline__ void vjp_pair(T *y, const VjpState<T> &P, const VjpState<T> &Qj, T dx, T dy,
-                                         T dz, T eps2, S self) {
+                                         T dz, T eps2, bool self) {
     const T rhoe = pn_fma(dz, dz, pn_fma(dy, dy, pn_fma(dx, dx, eps2)));
-    const T Q = vjp_self_mask(pn_rsqrt<T>(rhoe), self);
+    T Q = pn_rsqrt<T>(rhoe);
+    if (self) Q = T(0);
     const T Q2 = Q * Q, Q3 = Q2 * Q;
     const T vdp = pn_fma(P.vz, dz, pn_fma(P.vy, dy, P.vx * dx));     // v_p . d
     const T vdq = pn_fma(Qj.vz, dz, pn_fma(Qj.vy, dy, Qj.vx * dx));  // v_q . d
@@ -414,7 +408,7 @@ __global__ void __launch_bounds__(VJP_NT) k_pair_vjp(const PairVjpArgs a) {
                 dy = Qj.ey - P.ey;
                 dz = Qj.ez - P.ez;
             }
-            vjp_pair<T, bool>(F32 ? tacc : run, P, Qj, dx, dy, dz, (T)a.eps2, j == jself);
+            vjp_pair<T>(F32 ? tacc : run, P, Qj, dx, dy, dz, (T)a.eps2, j == jself);
         }
         if constexpr (F32)
             for (int q = 0; q < NY; ++q) kahan_add(run[q], cmp[q], tacc[q]);
@@ -430,186 +424,6 @@ __global__ void __launch_bounds__(VJP_NT) k_pair_vjp(const PairVjpArgs a) {
         for (int q = 0; q < NV_VJP; ++q) a.out[((size_t)split * NV_VJP + q) * a.npad + i] = o[q];
     }
 }
-
-// ------------------------------------------------------------------ the packed (mixed) sweep
-constexpr int VJP2_NG = 13;  // float4 groups of the duplicated pack (pn_vjp2.cuh)
-
-// Duplicated pack from the forward FP32 pack ([4][npad] float4) and the adjoint pack ([3][npad]).
-__global__ void __launch_bounds__(256) k_vjp_dup(const float4 *pack, const float4 *apack, float4 *dup,
-                                                 int npad, int nfill) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nfill) return;
-    const float4 g0 = pack[j], g1 = pack[npad + j], g2 = pack[2 * npad + j], g3 = pack[3 * npad + j];
-    const float4 a0 = apack[j], a1 = apack[npad + j], a2 = apack[2 * npad + j];
-    const float v[2 * VJP2_NG] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w, g2.x, g2.y, g2.z, g2.w,
-                                  g3.x, g3.y, g3.z, a2.y, a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w,
-                                  a2.x, a2.z};
-#pragma unroll
-    for (int g = 0; g < VJP2_NG; ++g) dup[(size_t)g * npad + j] = make_float4(v[2 * g], v[2 * g], v[2 * g + 1], v[2 * g + 1]);
-}
-
-__device__ __forceinline__ void vjp2_load(VjpState<V2> &S, const float4 *b, int tj, int j) {
-    f2 r[2 * VJP2_NG];
-#pragma unroll
-    for (int g = 0; g < VJP2_NG; ++g) lds2(b + (size_t)g * tj + j, r[2 * g], r[2 * g + 1]);
-    S.ex = V2::raw(r[0]); S.ey = V2::raw(r[1]); S.ez = V2::raw(r[2]); S.m = V2::raw(r[3]);
-    S.lx = V2::raw(r[4]); S.ly = V2::raw(r[5]); S.lz = V2::raw(r[6]); S.mu3 = V2::raw(r[7]);
-    S.vx = V2::raw(r[8]); S.vy = V2::raw(r[9]); S.vz = V2::raw(r[10]); S.qe = V2::raw(r[11]);
-    S.c1 = V2::raw(r[12]); S.c3 = V2::raw(r[13]); S.k35 = V2::raw(r[14]); S.vi2 = V2::raw(r[15]);
-    S.Gx = V2::raw(r[16]); S.Gy = V2::raw(r[17]); S.Gz = V2::raw(r[18]); S.Phi = V2::raw(r[19]);
-    S.Wx = V2::raw(r[20]); S.Wy = V2::raw(r[21]); S.Wz = V2::raw(r[22]); S.S0 = V2::raw(r[23]);
-    S.U = V2::raw(r[24]); S.cW = V2::raw(r[25]);
-}
-
-__device__ __forceinline__ V2 pk(float a, float b) { return V2::raw(f2_pack(a, b)); }
-
-// Two rows per thread (p0 = blockIdx.x * 256 + tid, p1 = p0 + 128), one per lane; tiles of tj
-// stars of the duplicated pack staged by the TMA engine (double buffered, bounded waits), the
-// j-range split over gridDim.y.  Row sums are Kahan-folded per tile into shared memory.
-template <bool MASK>
-__device__ __forceinline__ void vjp2_tile(V2 *tacc, const VjpState<V2> &P, const float4 *b, int tj, V2 eps2,
-                                          int jself0, int jself1) {
-#pragma unroll 1
-    for (int j = 0; j < tj; ++j) {
-        VjpState<V2> Qj;
-        vjp2_load(Qj, b, tj, j);
-        const V2 dx = (Qj.ex - P.ex) + (Qj.lx - P.lx);
-        const V2 dy = (Qj.ey - P.ey) + (Qj.ly - P.ly);
-        const V2 dz = (Qj.ez - P.ez) + (Qj.lz - P.lz);
-        if constexpr (MASK)
-            vjp_pair<V2, V2>(tacc, P, Qj, dx, dy, dz, eps2, pk(j == jself0 ? 0.f : 1.f, j == jself1 ? 0.f : 1.f));
-        else
-            vjp_pair<V2, bool>(tacc, P, Qj, dx, dy, dz, eps2, false);
-    }
-}
-
-__global__ void __launch_bounds__(VJP_NT, 1) k_pair_vjp2(const PairVjpArgs a) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
-    const int tj = a.tj;
-    float4 *buf = reinterpret_cast<float4 *>(smem + 128);
-    float *rc = reinterpret_cast<float *>(smem + 128 + 2 * (size_t)VJP2_NG * tj * 16);  // [NY][2 lanes][2][NT]
-    const int tid = threadIdx.x;
-    const int i0 = blockIdx.x * (2 * VJP_NT) + tid;
-    const int iv[2] = {i0, i0 + VJP_NT};
-    const int split = blockIdx.y;
-    const int t0 = (int)(((long long)a.ntiles * split) / a.gsplit);
-    const int t1 = (int)(((long long)a.ntiles * (split + 1)) / a.gsplit);
-    const float4 *pd = static_cast<const float4 *>(a.pack);   // duplicated pack [13][npad]
-    const float4 *pf = static_cast<const float4 *>(a.apack);  // forward pack [4][npad] (row state)
-    // row state of both lanes (the forward pack and the adjoint state in the duplicated pack)
-    VjpState<float> R[2];
-    double sx[2], sy[2], sz[2];
-    for (int k = 0; k < 2; ++k) {
-        const int i = iv[k];
-        const bool ok = i < a.nstar;
-        VjpState<float> &S = R[k];
-        S = VjpState<float>{};
-        sx[k] = sy[k] = sz[k] = 0.0;
-        if (ok) {
-            const float4 g1 = pf[i], g2 = pf[a.npad + i], g3 = pf[2 * a.npad + i], g4 = pf[3 * a.npad + i];
-            S.m = g1.w; S.mu3 = g2.w;
-            S.vx = g3.x; S.vy = g3.y; S.vz = g3.z; S.qe = g3.w;
-            S.c1 = g4.x; S.c3 = g4.y; S.k35 = g4.z;
-            const float4 d7 = pd[7 * (size_t)a.npad + i], d8 = pd[8 * (size_t)a.npad + i],
-                         d9 = pd[9 * (size_t)a.npad + i], d10 = pd[10 * (size_t)a.npad + i],
-                         d11 = pd[11 * (size_t)a.npad + i], d12 = pd[12 * (size_t)a.npad + i];
-            S.vi2 = d7.z; S.Gx = d8.x; S.Gy = d8.z; S.Gz = d9.x; S.Phi = d9.z;
-            S.Wx = d10.x; S.Wy = d10.z; S.Wz = d11.x; S.S0 = d11.z; S.U = d12.x; S.cW = d12.z;
-            sx[k] = a.spos[i];
-            sy[k] = a.spos[a.npad + i];
-            sz[k] = a.spos[2 * a.npad + i];
-        }
-    }
-    VjpState<V2> P;
-    P.vx = pk(R[0].vx, R[1].vx); P.vy = pk(R[0].vy, R[1].vy); P.vz = pk(R[0].vz, R[1].vz);
-    P.vi2 = pk(R[0].vi2, R[1].vi2); P.m = pk(R[0].m, R[1].m); P.mu3 = pk(R[0].mu3, R[1].mu3);
-    P.c1 = pk(R[0].c1, R[1].c1); P.c3 = pk(R[0].c3, R[1].c3); P.k35 = pk(R[0].k35, R[1].k35);
-    P.qe = pk(R[0].qe, R[1].qe);
-    P.Gx = pk(R[0].Gx, R[1].Gx); P.Gy = pk(R[0].Gy, R[1].Gy); P.Gz = pk(R[0].Gz, R[1].Gz);
-    P.Phi = pk(R[0].Phi, R[1].Phi); P.S0 = pk(R[0].S0, R[1].S0); P.U = pk(R[0].U, R[1].U);
-    P.Wx = pk(R[0].Wx, R[1].Wx); P.Wy = pk(R[0].Wy, R[1].Wy); P.Wz = pk(R[0].Wz, R[1].Wz);
-    P.cW = pk(R[0].cW, R[1].cW);
-    for (int q = 0; q < NY * 4; ++q) rc[(size_t)q * VJP_NT + tid] = 0.f;
-    if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    const uint32_t gbytes = (uint32_t)tj * 16u;
-    auto issue = [&](int t, int stage) {
-        mbar_arrive_expect_tx(&bars[stage], (uint32_t)VJP2_NG * gbytes);
-        for (int g = 0; g < VJP2_NG; ++g)
-            bulk_g2s(buf + (size_t)(stage * VJP2_NG + g) * tj, pd + (size_t)g * a.npad + (size_t)t * tj, gbytes,
-                     &bars[stage]);
-    };
-    if (tid == 0 && t0 < t1) issue(t0, 0);
-    const V2 eps2 = V2((float)a.eps2);
-    for (int t = t0; t < t1; ++t) {
-        const int it = t - t0, stage = it & 1;
-        const uint32_t phase = (uint32_t)(it >> 1) & 1u;
-        const bool next = t + 1 < t1;
-        if (tid == 0 && next) issue(t + 1, stage ^ 1);
-        const bool ok = mbar_wait_bounded(&bars[stage], phase);
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) {
-                atomicOr(a.err, DEVERR_TIMEOUT);
-                mbar_wait_bounded(&bars[stage], phase);
-                if (next) mbar_wait_bounded(&bars[stage ^ 1], (uint32_t)((it + 1) >> 1) & 1u);
-            }
-            return;
-        }
-        {
-            const TileOrigin o = a.torg[t];
-            float h[2][3], l[2][3];
-            for (int k = 0; k < 2; ++k) {
-                const double r[3] = {sx[k] - o.x, sy[k] - o.y, sz[k] - o.z};
-                for (int c = 0; c < 3; ++c) {
-                    h[k][c] = (float)r[c];
-                    l[k][c] = (float)(r[c] - (double)h[k][c]);
-                }
-            }
-            P.ex = pk(h[0][0], h[1][0]); P.ey = pk(h[0][1], h[1][1]); P.ez = pk(h[0][2], h[1][2]);
-            P.lx = pk(l[0][0], l[1][0]); P.ly = pk(l[0][1], l[1][1]); P.lz = pk(l[0][2], l[1][2]);
-        }
-        const float4 *b = buf + (size_t)stage * VJP2_NG * tj;
-        V2 tacc[NY];
-#pragma unroll
-        for (int q = 0; q < NY; ++q) tacc[q] = V2(0.f);
-        const int js0 = iv[0] - t * tj, js1 = iv[1] - t * tj;
-        if (__syncthreads_or((js0 >= 0 && js0 < tj) || (js1 >= 0 && js1 < tj)))
-            vjp2_tile<true>(tacc, P, b, tj, eps2, js0, js1);
-        else
-            vjp2_tile<false>(tacc, P, b, tj, eps2, js0, js1);
-#pragma unroll
-        for (int q = 0; q < NY; ++q)
-            for (int k = 0; k < 2; ++k) {
-                float *run = &rc[(size_t)((q * 2 + k) * 2) * VJP_NT + tid];
-                float *cmp = run + VJP_NT;
-                float su = *run, co = *cmp;
-                kahan_add(su, co, lane(tacc[q], k));
-                *run = su;
-                *cmp = co;
-            }
-        __syncthreads();
-    }
-    for (int k = 0; k < 2; ++k) {
-        const int i = iv[k];
-        if (i >= a.nstar) continue;
-        double Y[NY], o[NV_VJP];
-        for (int q = 0; q < NY; ++q) {
-            const float *run = &rc[(size_t)((q * 2 + k) * 2) * VJP_NT + tid];
-            Y[q] = (double)run[0] - (double)run[VJP_NT];
-        }
-        const int tself = i / tj;
-        const bool has_self = tself >= t0 && tself < t1;
-        vjp_row_out<float>(o, Y, R[k], has_self ? 1.0 / sqrt(a.eps2) : 0.0);
-        for (int q = 0; q < NV_VJP; ++q) a.out[((size_t)split * NV_VJP + q) * a.npad + i] = o[q];
-    }
-}
-
-inline size_t vjp2_smem(int tj) { return 128 + 2 * (size_t)VJP2_NG * tj * 16 + (size_t)NY * 4 * VJP_NT * 4; }
 
 // ------------------------------------------------------------------ assembly
 struct AssembleArgs {
@@ -752,7 +566,6 @@ struct AdjointWork {
     double *ckpt = nullptr;     // [nck][6][ld]  (x, v at steps 0, K, 2K, ...)
     double *seg = nullptr;      // [K][3][6][ld] evaluation states of a segment's stages
     double *segsums = nullptr;  // [K][3][9][npad]
-    float4 *dup = nullptr;      // mixed precision: the duplicated pack of the packed sweep [13][npad]
     int seg_holds = -1;         // segment whose stages seg/segsums hold (-1: none)
     double time0 = 0.0;
 };
@@ -763,7 +576,7 @@ void free_adjoint(pn_ctx *c) {
     AdjointWork *w = c->adj;
     if (!w) return;
     void *b[] = {w->sums, w->apack, w->sdir, w->vdir, w->vjp, w->gbar, w->part, w->m0bar, w->tickets,
-                 w->work, w->ckpt, w->seg, w->segsums, w->dup};
+                 w->work, w->ckpt, w->seg, w->segsums};
     for (void *p : b)
         if (p) cudaFree(p);
     delete w;
@@ -836,8 +649,7 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
     CU(cudaGetLastError());
     // O(N^2) sweep
     const int ntiles = nstar > 0 ? (nstar + tj - 1) / tj : 0;
-    const int rows_per_block = f32 ? 2 * VJP_NT : VJP_NT;  // the packed sweep: two rows per thread
-    const int nib = (nstar + rows_per_block - 1) / rows_per_block;
+    const int nib = (nstar + VJP_NT - 1) / VJP_NT;
     int g = nib > 0 ? (4 * 152 * 6 + nib - 1) / nib : 1;
     if (g > 32) g = 32;
     if (g > ntiles) g = ntiles;
@@ -859,24 +671,8 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
         qa.eps2 = eps2;
         dim3 grid((unsigned)nib, (unsigned)g);
         if (f32) {
-            if (!w->dup && cudaMalloc(&w->dup, (size_t)VJP2_NG * c->npad * 16) != cudaSuccess) {
-                cudaGetLastError();
-                return set_err(PN_ERR_NOMEM, "vjp pack");
-            }
-            k_vjp_dup<<<(pa.nfill + 255) / 256, 256, 0, s>>>(static_cast<const float4 *>(c->pack),
-                                                               static_cast<const float4 *>(w->apack), w->dup,
-                                                               c->npad, pa.nfill);
-            CU(cudaGetLastError());
-            const size_t smem = vjp2_smem(tj);
-            static size_t configured = 0;
-            if (smem > configured) {
-                CU(cudaFuncSetAttribute(k_pair_vjp2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                configured = smem;
-            }
-            PairVjpArgs q2 = qa;
-            q2.pack = w->dup;     // j data: the duplicated pack
-            q2.apack = c->pack;   // row data: the forward pack
-            k_pair_vjp2<<<grid, VJP_NT, smem, s>>>(q2);
+            const size_t smem = 128 + 2 * (size_t)(VjpPack<float>::NGF + VjpPack<float>::NGA) * tj * 16;
+            k_pair_vjp<float><<<grid, VJP_NT, smem, s>>>(qa);
         } else {
             const size_t smem = 128 + 2 * (size_t)(VjpPack<double>::NGF + VjpPack<double>::NGA) * tj * 16;
             k_pair_vjp<double><<<grid, VJP_NT, smem, s>>>(qa);
