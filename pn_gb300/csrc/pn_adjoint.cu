@@ -672,9 +672,19 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
         dim3 grid((unsigned)nib, (unsigned)g);
         if (f32) {
             const size_t smem = 128 + 2 * (size_t)(VjpPack<float>::NGF + VjpPack<float>::NGA) * tj * 16;
+            static size_t configured = 0;
+            if (smem > 48 * 1024 && smem > configured) {
+                CU(cudaFuncSetAttribute(k_pair_vjp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                configured = smem;
+            }
             k_pair_vjp<float><<<grid, VJP_NT, smem, s>>>(qa);
         } else {
             const size_t smem = 128 + 2 * (size_t)(VjpPack<double>::NGF + VjpPack<double>::NGA) * tj * 16;
+            static size_t configured = 0;
+            if (smem > 48 * 1024 && smem > configured) {
+                CU(cudaFuncSetAttribute(k_pair_vjp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                configured = smem;
+            }
             k_pair_vjp<double><<<grid, VJP_NT, smem, s>>>(qa);
         }
         CU(cudaGetLastError());
