@@ -37,6 +37,10 @@ namespace pn {
 enum VjpSlot : int { V_SX = 0, V_SY, V_SZ, V_VX, V_VY, V_VZ, V_QE, V_MU3, V_C1, V_C3, V_K35, NV_VJP };
 enum GbarSlot : int { GB_A1 = 0, GB_B3X, GB_B3Y, GB_B3Z, GB_C, GB_PX, GB_PY, GB_PZ, GB_M0, NGBAR };
 
+// Threads per block of the O(N) adjoint kernels: their per-star FP64 work is heavy, so small
+// blocks spread a system of a few thousand stars over every SM.
+constexpr int VJP_ON_NT = 64;
+
 // ------------------------------------------------------------------ per-star adjoint
 struct FinVjpArgs {
     const double *spos, *v, *m, *sums, *glob;
@@ -601,7 +605,7 @@ static int adj_ensure(pn_ctx *c) {
     };
     const bool ok = mal((void **)&w->sums, 9 * np * 8) && mal(&w->apack, 6 * np * 16) &&
                     mal((void **)&w->sdir, 3 * np * 8) && mal((void **)&w->vdir, 3 * np * 8) &&
-                    mal((void **)&w->gbar, 16 * 8) && mal((void **)&w->part, (np / 256 + 2) * 16 * 8) &&
+                    mal((void **)&w->gbar, 16 * 8) && mal((void **)&w->part, (np / VJP_ON_NT + 2) * 16 * 8) &&
                     mal((void **)&w->m0bar, 2 * 8) && mal((void **)&w->tickets, 4 * sizeof(unsigned)) &&
                     mal((void **)&w->work, 12 * 3 * ld * 8);
     if (!ok) {
@@ -644,8 +648,8 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
     fa.eps = c->p.eps; fa.eps2 = eps2; fa.ic2 = c->p.inv_c2;
     fa.apack = w->apack; fa.sdir = w->sdir; fa.vdir = w->vdir; fa.part = w->part; fa.gbar = w->gbar;
     fa.ticket = &w->tickets[0];
-    const int nbf = (pa.nfill + 255) / 256;
-    k_finish_vjp<<<nbf, 256, 0, s>>>(fa);
+    const int nbf = (pa.nfill + VJP_ON_NT - 1) / VJP_ON_NT;
+    k_finish_vjp<<<nbf, VJP_ON_NT, 0, s>>>(fa);
     CU(cudaGetLastError());
     // O(N^2) sweep
     const int ntiles = nstar > 0 ? (nstar + tj - 1) / tj : 0;
@@ -695,8 +699,8 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
     aa.xbar = xbar; aa.vbar = vbar; aa.osp = 1; aa.osk = ld; aa.accumulate = accumulate;
     aa.m0_accumulate = m0_accumulate;
     aa.part = w->part; aa.m0bar = m0bar; aa.ticket = &w->tickets[1];
-    const int nba = nstar > 0 ? (nstar + 255) / 256 : 1;
-    k_vjp_assemble<<<nba, 256, 0, s>>>(aa);
+    const int nba = nstar > 0 ? (nstar + VJP_ON_NT - 1) / VJP_ON_NT : 1;
+    k_vjp_assemble<<<nba, VJP_ON_NT, 0, s>>>(aa);
     CU(cudaGetLastError());
     return PN_OK;
 }
