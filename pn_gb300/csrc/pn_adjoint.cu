@@ -562,6 +562,7 @@ struct AdjointWork {
     void *apack = nullptr;   // [6][npad] x 16 B
     double *sdir = nullptr, *vdir = nullptr, *vjp = nullptr, *gbar = nullptr, *part = nullptr;
     int vjp_splits = 0;
+    int g_best = 1, g_nstar = -1, g_f32 = -1;  // split count of the VJP sweep for this size
     double *m0bar = nullptr;
     unsigned *tickets = nullptr;
     double *work = nullptr;  // [12][3][ld]: Xb Vb xb vb x1b v1b x2b v2b ab xF vF spare
@@ -654,10 +655,32 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
     // O(N^2) sweep
     const int ntiles = nstar > 0 ? (nstar + tj - 1) / tj : 0;
     const int nib = (nstar + VJP_NT - 1) / VJP_NT;
-    int g = nib > 0 ? (4 * 152 * 6 + nib - 1) / nib : 1;
-    if (g > 32) g = 32;
-    if (g > ntiles) g = ntiles;
-    if (g < 1) g = 1;
+    // j-range splits: the count whose CTAs fill the resident slots in the fewest tile-times,
+    // waves x tiles per CTA (a wave of small systems leaves SMs idle otherwise)
+    if (w->g_nstar != nstar || w->g_f32 != (int)f32) {
+        int dev = 0, sms = 0, per = 0;
+        CU(cudaGetDevice(&dev));
+        CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const size_t smem = 128 + 2 * (size_t)(f32 ? VjpPack<float>::NGF + VjpPack<float>::NGA
+                                                    : VjpPack<double>::NGF + VjpPack<double>::NGA) * tj * 16;
+        CU(f32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pair_vjp<float>, VJP_NT, smem)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pair_vjp<double>, VJP_NT, smem));
+        const long long slots = (long long)sms * (per > 0 ? per : 1);
+        int best = 1;
+        long long best_cost = -1;
+        for (int gc = 1; gc <= 64 && gc <= (ntiles > 0 ? ntiles : 1); ++gc) {
+            const long long waves = ((long long)nib * gc + slots - 1) / slots;
+            const long long cost = waves * ((ntiles + gc - 1) / gc);
+            if (best_cost < 0 || cost < best_cost) {
+                best_cost = cost;
+                best = gc;
+            }
+        }
+        w->g_best = best;
+        w->g_nstar = nstar;
+        w->g_f32 = (int)f32;
+    }
+    const int g = w->g_best;
     if (g > w->vjp_splits) {
         if (w->vjp) cudaFree(w->vjp);
         w->vjp = nullptr;
