@@ -350,11 +350,12 @@ def run_adjoint(args):
     gx1, gv1, gm1 = grads[1]
     dmix = np.sqrt((np.linalg.norm(gx1 - gx) ** 2 + np.linalg.norm(gv1 - gv) ** 2) /
                    (np.linalg.norm(gx) ** 2 + np.linalg.norm(gv) ** 2))
-    line = {"metric": f"adjoint cost per step / forward step (N={ns}, {nsteps} steps, mixed)",
-            "value": timing["mixed"]["ratio_K20"], "unit": "ratio", "n_gpus": 1, "steps": nsteps,
+    line = {"metric": f"adjoint backward cost per step / forward step (N={ns}, {nsteps} steps, mixed, "
+                      f"every stage kept in HBM)",
+            "value": timing["mixed"][f"ratio_K{nsteps}"], "unit": "ratio", "n_gpus": 1, "steps": nsteps,
             "warmup": 2, "higher_is_better": False, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": f"plummer_bh_N{ns}_adjoint", "bh_mass_fraction": 0.05, "dt": DT,
-                       "checkpoint_every": 20, "inv_c2": INV_C2},
+                       "checkpoint_every": nsteps, "also_timed_checkpoint_every": 20, "inv_c2": INV_C2},
             "timing": timing,
             "fd_check_fp64": {"steps": fs, "h": h, "coords": len(checks), "max_rel_err": float(max(checks)),
                               "median_rel_err": float(np.median(checks)),
