@@ -152,7 +152,7 @@ int pn_get_stats(pn_ctx *ctx, pn_stats *s);
 /* Changes the run parameters of an existing context (e.g. precision). */
 int pn_set_params(pn_ctx *ctx, const pn_params *p);
 
-/* Binary checkpoint of a context (state, masses, time, parameters) plus the driver's snapshot
+/* Binary checkpoint of a context (state, masses, time, parameters) plus the calling loop's snapshot
  * clock and initial energy; pn_load_checkpoint restores all of it into an existing context
  * (n must fit its capacity).  Format: "PNCK0001", int32 n, doubles time, eouttime, init_ene,
  * the pn_params struct, then x, v (AoS [n][3]) and m [n], little-endian. */
