@@ -19,8 +19,21 @@ interactions.
   cpu_baseline the oracle port of the reference (bit-identical to it) on a bounded sample of
                rows of force() on the host cores, scaled to interactions/s
 
+On one GPU the same JSON line also carries the other configurations of the workload set, each
+run within a share of a wall-clock budget (--budget-s, default 25 min for the whole command;
+a leg that would overrun stops early and says how far it got):
+
+  config4      256 clusters, N log-uniform in [1024, 65536], in one persistent launch per force
+               evaluation (mixed), K timed steps; clusters checked against individual FP64 runs
+  config5      the discrete adjoint at N = 16,384 over 200 steps: backward cost per step over a
+               forward step with checkpoints every 20 steps and with every stage kept, mixed and
+               FP64; the FP64 gradient against central differences (h = 1e-6) on 64 coordinates
+               and the BH mass, with a Richardson pair (h/2) on the worst ones
+  config2      N = 65,536 Plummer + BH, 500 steps in FP64 and in mixed precision: throughput and
+               the two energy-drift curves (every 50 steps)
+
 --impl reference times the reference's CPU implementation of the path (the oracle port; the
-reference itself cannot be built on the GPU host) on all host cores, a bounded sample per step.
+reference itself cannot be built on the GPU host) on one core, as the reference runs.
 """
 from __future__ import annotations
 
@@ -48,15 +61,32 @@ DT = 1.0 / 1024.0
 INV_C2 = 1e-6
 METRIC = "interactions/s at N=2^18 (mixed FP32/FP64 integration step)"
 UNIT = "interactions/s"
+T_START = time.monotonic()
 
 
-def workload_config(nstars=NSTARS):
-    import pn_gb300 as pn
+class Budget:
+    """Wall-clock budget of the whole command (seconds from process start)."""
+
+    def __init__(self, seconds):
+        self.end = T_START + seconds
+
+    def left(self):
+        return self.end - time.monotonic()
+
+
+def plummer_eps(nstars):
+    """Softening 0.01 * 4 / N^(1/3) of the Plummer configurations."""
+    return 0.01 * 4.0 / nstars ** (1.0 / 3.0)
+
+
+def workload_config(nstars=NSTARS, world=1):
+    """The workload both arms time (the same keys and values in both lines)."""
     return {"workload": f"plummer_bh_N{nstars}", "n_particles": nstars + 1,
-            "bh_mass_fraction": BH_FRACTION, "eps": pn.plummer_eps(nstars), "dt": DT,
+            "bh_mass_fraction": BH_FRACTION, "eps": plummer_eps(nstars), "dt": DT,
             "inv_c2": INV_C2, "step": "3 force() evaluations + stage updates (Limit-sticky9.c:844-893)",
             "interaction": "one Newtonian (i,j) pair, n^2 per force()",
-            "l2": "2x L2 overwritten before each timed step"}
+            "l2": "2x L2 overwritten before each timed step",
+            "parallelism": f"replicas{world}" if world > 1 else "1 GPU"}
 
 
 def _measured_hbm_gbs():
@@ -154,21 +184,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(sysm, eps, seconds=12.0, threads=None):
+def cpu_baseline(x, v, m, eps, seconds=12.0, threads=None):
     """The oracle port on a bounded sample of force() rows (all three O(N^2) sweeps of each
     row), timed on the host cores; returns interactions/s and the sample description."""
     from oracle import pyoracle as po
     po.build(ref=False)
     threads = threads or os.cpu_count() or 1
-    n = sysm.x.shape[0]
+    n = x.shape[0]
     rng = np.random.default_rng(1)
     rows = np.sort(rng.choice(np.arange(1, n), size=threads * 2, replace=False))
-    t = po.time_force_rows(sysm.x, sysm.v, sysm.m, eps, rows, threads)  # calibration
+    t = po.time_force_rows(x, v, m, eps, rows, threads)  # calibration
     per_row = t / rows.size * threads
     k = max(threads, int(seconds * threads / max(per_row, 1e-6)))
     k = min(k, n - 1)
     rows = np.sort(rng.choice(np.arange(1, n), size=k, replace=False))
-    t = po.time_force_rows(sysm.x, sysm.v, sysm.m, eps, rows, threads)
+    t = po.time_force_rows(x, v, m, eps, rows, threads)
     rate = rows.size * n / t
     return rate, {"rows": int(rows.size), "seconds": t, "threads": threads,
                   "sample": f"{rows.size} random rows of force() at N={n - 1} (Newtonian row, "
@@ -176,50 +206,60 @@ def cpu_baseline(sysm, eps, seconds=12.0, threads=None):
                             f"interactions = rows x n"}
 
 
-def run_reference(args, rank, world, dist):
-    """--impl reference: the reference's CPU path (oracle port) on all host cores."""
-    import pn_gb300 as pn
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU implementation of the path (the oracle port,
+    bit-identical to Limit-sticky9.c's force(); the reference source is not on the GPU host) on
+    this host's cores.  The reference is single-threaded as shipped (its OpenMP pragma is
+    commented out, Limit-sticky9.c:34), so `value` is one core; the same sample on every host
+    thread is reported beside it.  The input is the same Plummer + BH workload, sampled by the
+    oracle's own numpy generator: this arm loads no part of libpn."""
     if rank != 0:
         return 0
-    sysm = pn.config_plummer(NSTARS, SEED, BH_FRACTION)
-    eps = pn.plummer_eps(NSTARS)
-    threads = os.cpu_count() or 1
     from oracle import pyoracle as po
     po.build(ref=False)
-    n = sysm.x.shape[0]
+    x, v, m = po.plummer_bh(NSTARS, SEED, BH_FRACTION)
+    eps = plummer_eps(NSTARS)
+    n = x.shape[0]
     rng = np.random.default_rng(7)
-    rows_per_step = threads * 4
+    # rows per step: about 0.25 s of one core (calibrated on a few rows)
+    t = po.time_force_rows(x, v, m, eps, np.sort(rng.choice(np.arange(1, n), 4, replace=False)), 1)
+    rows_per_step = int(min(max(2, 0.25 / max(t / 4, 1e-6)), 4096))
     times = []
-    for s in range(args.warmup + args.steps):
+    for s_ in range(args.warmup + args.steps):
         rows = np.sort(rng.choice(np.arange(1, n), size=rows_per_step, replace=False))
-        t = po.time_force_rows(sysm.x, sysm.v, sysm.m, eps, rows, threads)
-        if s >= args.warmup:
+        t = po.time_force_rows(x, v, m, eps, rows, 1)
+        if s_ >= args.warmup:
             times.append(t)
     total = sum(times)
     value = args.steps * rows_per_step * n / total
+    threads = os.cpu_count() or 1
+    rows = np.sort(rng.choice(np.arange(1, n), size=min(n - 1, rows_per_step * threads * 4), replace=False))
+    t_all = po.time_force_rows(x, v, m, eps, rows, threads)
+    sample = (f"{rows_per_step} random rows of force() per step (all three O(N^2) sweeps per row, "
+              f"n interactions each), 1 thread as the reference runs; the reference source is not "
+              f"on the GPU host, so the bit-identical C port of it runs")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded Plummer sphere + BH)", "config": workload_config(),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{rows_per_step} random rows of force() per step "
-                                       f"(all three O(N^2) sweeps per row), {threads} threads; "
-                                       "the reference source is not on the GPU host, so the "
-                                       "bit-identical C port of it runs"},
+            "data": "synthetic (seeded Plummer sphere + BH)", "config": workload_config(NSTARS, world),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample,
+                             "all_threads_value": rows.size * n / t_all, "all_threads": threads},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def run_ensemble(args):
-    """Configuration 4: 256 Plummer + BH clusters, N log-uniform in [1024, 65536], BH mass
-    fraction log-uniform in [1e-3, 1e-1], eps = 0.01, dt = 1/1024, mixed precision, one
-    persistent pair launch per force evaluation, each step one CUDA graph.  Times K steps
-    (interactions/s = sum n_c^2 per evaluation, 3 per step) and checks a subset of clusters
-    against individual FP64 runs."""
+# ---------------------------------------------------------------------------- configuration 4
+def ensemble_leg(steps, warmup, nclusters, allowance):
+    """256 Plummer + BH clusters, N log-uniform in [1024, 65536], BH mass fraction log-uniform in
+    [1e-3, 1e-1], eps = 0.01, dt = 1/1024, mixed precision, one persistent pair launch per force
+    evaluation, each step one CUDA graph.  Times `steps` steps (interactions/s = sum n_c^2 per
+    evaluation, 3 per step) and checks clusters (the smallest, the largest and random ones)
+    against individual FP64 runs of the same number of steps."""
     import pn_gb300 as pn
+    t_leg = time.monotonic()
     rng = np.random.default_rng(4)
-    nc = args.clusters
+    nc = nclusters
     sizes = np.exp(rng.uniform(np.log(1024), np.log(65536), nc)).astype(int)
     fracs = np.exp(rng.uniform(np.log(1e-3), np.log(1e-1), nc))
     systems = [pn.config_plummer(int(s), 1000 + k, float(f)) for k, (s, f) in enumerate(zip(sizes, fracs))]
@@ -229,66 +269,76 @@ def run_ensemble(args):
     t0 = time.perf_counter()
     e.autotune()
     tune_s = time.perf_counter() - t0
-    e.bench_steps(args.warmup)
+    e.bench_steps(warmup)
     with ClockSampler() as clk:
-        ms = e.bench_steps(args.steps)
+        ms = e.bench_steps(steps)
     total = float(ms.sum())
-    # cluster-by-cluster check: the ensemble (mixed) after the warm-up and timed steps against
-    # individual FP64 contexts run for the same number of steps
-    nsteps = args.warmup + args.steps
+    nsteps = warmup + steps
     xs, vs = e.get_state()
     e.close()
-    picks = sorted(set([int(np.argmin(sizes)), int(np.argmax(sizes))] + list(rng.choice(nc, 4, replace=False))))
-    errs = {}
+    picks = [int(np.argmin(sizes)), int(np.argmax(sizes))]
+    picks += [int(k) for k in rng.choice(nc, 6, replace=False) if int(k) not in picks]
+    errs, skipped = {}, []
     for k in picks:
         s = systems[k]
+        # an individual FP64 run costs ~n^2 / 1.1e10 s per evaluation on this GPU
+        est = 3.0 * nsteps * float(s.x.shape[0]) ** 2 / 1.0e10
+        if time.monotonic() - t_leg + est > allowance:
+            skipped.append(k)
+            continue
         with pn.Context(s.x.shape[0], eps=eps[k], dt=DT, inv_c2=INV_C2) as c:
             c.set_state(s.x, s.v, s.m)
             c.steps(nsteps)
             xr, vr = c.get_state()
-        errs[str(k)] = {"n": int(s.x.shape[0]),
+        errs[str(k)] = {"n": int(s.x.shape[0]), "bh_fraction": float(fracs[k]),
                         "max_pos_err_rel": float(np.abs(xs[k] - xr).max() / np.abs(xr).max()),
                         "max_vel_err_rel": float(np.abs(vs[k] - vr).max() / np.abs(vr).max())}
-    line = {"metric": "interactions/s, ensemble of 256 clusters (persistent launch, CUDA graph steps)",
-            "value": args.steps * inter / (total * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+    return {"metric": f"interactions/s, ensemble of {nc} clusters (persistent launch, CUDA graph steps)",
+            "value": steps * inter / (total * 1e-3), "unit": UNIT, "steps": steps, "warmup": warmup,
+            "ms_per_step": total / steps, "dtype": "f32+f64", "gpu_launches": 3 * 3 * steps,
             "config": {"workload": f"ensemble_{nc}_plummer_bh", "n_range": [int(sizes.min()), int(sizes.max())],
                        "particles": int(sum(s.x.shape[0] for s in systems)), "eps": 0.01, "dt": DT,
                        "inv_c2": INV_C2, "autotune_s": tune_s},
-            "clocks": clk.summary(), "check_vs_individual_fp64": errs}
-    print(json.dumps(line), flush=True)
-    return 0
+            "clocks": clk.summary(),
+            "check_vs_individual_fp64": {"steps": nsteps, "clusters": errs, "skipped_for_time": skipped,
+                                         "max_pos_err_rel": max((v["max_pos_err_rel"] for v in errs.values()), default=None),
+                                         "max_vel_err_rel": max((v["max_vel_err_rel"] for v in errs.values()), default=None)},
+            "seconds": time.monotonic() - t_leg}
 
 
-def run_adjoint(args):
-    """Configuration 5: N = 16384 Plummer + BH (mass fraction 0.05), 200 steps at dt = 1/1024.
-    Loss: squared distance of the final snapshot (x, v) to a target made with the BH mass x 1.1
-    and initial positions + N(0, 1e-3^2).  Reports the cost of the adjoint per step against a
-    forward step (mixed and FP64) with checkpoints every 20 steps (segments recomputed) and with
-    every stage kept (checkpoint interval = steps, no recomputation: 1.2 GB of HBM here).
-    The FP64 gradient is checked against central differences (h = 1e-6) on sampled coordinates
-    and the BH mass over --fd-steps steps: over 200 steps at this dt the close BH passages make
-    the loss too nonlinear in the inputs for any step h to converge (h = 1e-4 .. 1e-7 disagree
-    with each other by more than 100 %), over 40 steps the differences converge to the adjoint
-    (~1e-9 at h = 1e-6).  The mixed-precision gradient is compared with the FP64 one."""
+# ---------------------------------------------------------------------------- configuration 5
+def adjoint_leg(ns, nsteps, fd_steps, fd_coords, allowance, richardson=6):
+    """N = 16384 Plummer + BH (mass fraction 0.05), 200 steps at dt = 1/1024.  Loss: squared
+    distance of the final snapshot (x, v) to a target made with the BH mass x 1.1 and initial
+    positions + N(0, 1e-3^2).
+
+    Cost: the backward pass per step over a forward step, mixed and FP64, with checkpoints every
+    20 steps (the backward pass recomputes each segment but the last from its checkpoint) and
+    with every stage kept (checkpoint interval = steps: nothing recomputed).
+
+    Finite differences (FP64, h = 1e-6) over `fd_steps` steps: over 200 steps at this dt the
+    close BH passages make the loss too nonlinear in the inputs for any h to converge (h = 1e-4
+    .. 1e-7 disagree by more than 100 %); over 40 steps they converge.  Coordinates: half at
+    random among the stars' positions and velocities, half the largest |g|, plus the BH mass.
+    Errors are reported normwise, |g_i - fd_i| / max|g| (the adjoint's largest component), and
+    per coordinate for the largest-|g| half; the worst coordinates get a second difference at
+    h/2 (Richardson pair): truncation error scales as h^2, round-off as 1/h.  The mixed-precision
+    gradient is compared with the FP64 one."""
     import pn_gb300 as pn
-    ns, nsteps = args.adj_n, args.adj_steps
+    t_leg = time.monotonic()
     s = pn.config_plummer(ns, 77, 0.05)
-    eps = pn.plummer_eps(ns)
+    eps = plummer_eps(ns)
     rng = np.random.default_rng(5)
     n = ns + 1
-
-    def final(x, v, m, steps, prec=0):
-        with pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=prec) as c:
-            c.set_state(x, v, m)
-            c.steps(steps)
-            return c.get_state()
-
     mt = s.m.copy()
     mt[0] *= 1.1
     xt0 = s.x + rng.normal(0, 1e-3, s.x.shape)
     xt0[0] = s.x[0]
+
+    def final(c, x, v, m, steps):
+        c.set_state(x, v, m)
+        c.steps(steps)
+        return c.get_state()
 
     def gradient(c, steps, K, xT, vT):
         c.set_state(s.x, s.v, s.m)
@@ -298,7 +348,15 @@ def run_adjoint(args):
         g = c.adjoint_backward(2 * (xe - xT), 2 * (ve - vT))
         return g, (time.perf_counter() - t0) / steps
 
-    xT, vT = final(xt0, s.v, mt, nsteps)
+    out = {"metric": f"adjoint backward cost per step / forward step (N={ns}, {nsteps} steps, "
+                     f"checkpoints every 20 steps, mixed)", "unit": "ratio", "higher_is_better": False,
+           "config": {"workload": f"plummer_bh_N{ns}_adjoint", "bh_mass_fraction": 0.05, "dt": DT,
+                      "steps": nsteps, "checkpoint_every": 20, "also_timed_checkpoint_every": nsteps,
+                      "inv_c2": INV_C2, "loss": "|x(T)-x*(T)|^2 + |v(T)-v*(T)|^2, target: m_BH x 1.1, "
+                                                "x0 + N(0, 1e-3^2)"}}
+    with pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=pn.PN_PREC_MIXED) as c:
+        xT, vT = final(c, xt0, s.v, mt, nsteps)  # the target (any precision: it is data)
+        xTf, vTf = final(c, xt0, s.v, mt, fd_steps)
     timing = {}
     for prec in (1, 0):
         with pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=prec) as c:
@@ -314,88 +372,135 @@ def run_adjoint(args):
                 r[f"adj_ms_per_step_K{K}"] = bwd * 1e3
                 r[f"ratio_K{K}"] = bwd / fwd
             timing["mixed" if prec else "fp64"] = r
-    # finite-difference check (FP64) over fd_steps steps
-    fs = args.fd_steps
-    xTf, vTf = final(xt0, s.v, mt, fs)
-
-    def loss(x, v, m):
-        xe, ve = final(x, v, m, fs)
-        return float(((xe - xTf) ** 2).sum() + ((ve - vTf) ** 2).sum())
-
+    out["value"] = timing["mixed"]["ratio_K20"]
+    out["timing"] = timing
+    # gradients over the finite-difference horizon, FP64 and mixed
     grads = {}
     for prec in (0, 1):
         with pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=prec) as c:
-            grads[prec], _ = gradient(c, fs, 20, xTf, vTf)
+            grads[prec], _ = gradient(c, fd_steps, 20, xTf, vTf)
     gx, gv, gm = grads[0]
-    h = 1e-6
-    checks = []
-    for q in rng.choice(np.arange(3, 6 * n), args.fd_coords, replace=False):
-        which, r_ = divmod(int(q), 3 * n)
-        p_, k = divmod(r_, 3)
-        if p_ == 0:
-            continue
-        a = (s.x if which == 0 else s.v).copy()
-        b = a.copy()
-        a[p_, k] += h
-        b[p_, k] -= h
-        lp = loss(a, s.v, s.m) if which == 0 else loss(s.x, a, s.m)
-        lm = loss(b, s.v, s.m) if which == 0 else loss(s.x, b, s.m)
-        fd = (lp - lm) / (2 * h)
-        g = (gx if which == 0 else gv)[p_, k]
-        checks.append(abs(g - fd) / max(abs(fd), 1e-300))
-    mp, mm = s.m.copy(), s.m.copy()
-    mp[0] += h
-    mm[0] -= h
-    fdm = (loss(s.x, s.v, mp) - loss(s.x, s.v, mm)) / (2 * h)
     gx1, gv1, gm1 = grads[1]
-    dmix = np.sqrt((np.linalg.norm(gx1 - gx) ** 2 + np.linalg.norm(gv1 - gv) ** 2) /
-                   (np.linalg.norm(gx) ** 2 + np.linalg.norm(gv) ** 2))
-    line = {"metric": f"adjoint backward cost per step / forward step (N={ns}, {nsteps} steps, mixed, "
-                      f"every stage kept in HBM)",
-            "value": timing["mixed"][f"ratio_K{nsteps}"], "unit": "ratio", "n_gpus": 1, "steps": nsteps,
-            "warmup": 2, "higher_is_better": False, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": f"plummer_bh_N{ns}_adjoint", "bh_mass_fraction": 0.05, "dt": DT,
-                       "checkpoint_every": nsteps, "also_timed_checkpoint_every": 20, "inv_c2": INV_C2},
-            "timing": timing,
-            "fd_check_fp64": {"steps": fs, "h": h, "coords": len(checks), "max_rel_err": float(max(checks)),
-                              "median_rel_err": float(np.median(checks)),
-                              "bh_mass_rel_err": float(abs(gm - fdm) / abs(fdm))},
-            "mixed_vs_fp64_grad_rel": float(dmix), "mixed_vs_fp64_dm0_rel": float(abs(gm1 / gm - 1))}
-    print(json.dumps(line), flush=True)
-    return 0
+    out["mixed_vs_fp64_grad_rel"] = float(np.sqrt((np.linalg.norm(gx1 - gx) ** 2 + np.linalg.norm(gv1 - gv) ** 2) /
+                                                  (np.linalg.norm(gx) ** 2 + np.linalg.norm(gv) ** 2)))
+    out["mixed_vs_fp64_dm0_rel"] = float(abs(gm1 / gm - 1))
+    gall = np.concatenate([gx[1:].ravel(), gv[1:].ravel()])  # stars' coordinates
+    gmax = float(np.abs(gall).max())
+    half = fd_coords // 2
+    top = np.argsort(-np.abs(gall))[:half]
+    rest = np.setdiff1d(np.arange(gall.size), top)
+    rnd = rng.choice(rest, fd_coords - half, replace=False)
+    h = 1e-6
+    with pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=pn.PN_PREC_FP64) as c:
+        c.set_state(s.x, s.v, s.m)
+        c.steps(1)  # warm-up
+
+        def loss(x, v, m):
+            xe, ve = final(c, x, v, m, fd_steps)
+            return float(((xe - xTf) ** 2).sum() + ((ve - vTf) ** 2).sum())
+
+        def fd_coord(q, hh):
+            which, r_ = divmod(int(q), 3 * ns)
+            p_, k = divmod(r_, 3)
+            p_ += 1  # stars are rows 1..ns
+            a = (s.x if which == 0 else s.v).copy()
+            b = a.copy()
+            a[p_, k] += hh
+            b[p_, k] -= hh
+            lp = loss(a, s.v, s.m) if which == 0 else loss(s.x, a, s.m)
+            lm = loss(b, s.v, s.m) if which == 0 else loss(s.x, b, s.m)
+            return (lp - lm) / (2 * hh), ("x" if which == 0 else "v", p_, k)
+
+        def fd_mass(hh):
+            mp, mm = s.m.copy(), s.m.copy()
+            mp[0] += hh
+            mm[0] -= hh
+            return (loss(s.x, s.v, mp) - loss(s.x, s.v, mm)) / (2 * hh)
+
+        t1 = time.perf_counter()
+        fdm = fd_mass(h)
+        per_loss = (time.perf_counter() - t1) / 2
+        rows, skipped = [], 0
+        for kind, qs in (("top_abs_g", top), ("random", rnd)):
+            for q in qs:
+                if time.monotonic() - t_leg + 2 * per_loss > allowance:
+                    skipped += 1
+                    continue
+                fd, (var, p_, k) = fd_coord(q, h)
+                g = float(gall[q])
+                rows.append({"kind": kind, "var": var, "particle": int(p_), "k": int(k), "g": g, "fd": float(fd),
+                             "err_normwise": abs(g - fd) / gmax, "err_rel": abs(g - fd) / max(abs(fd), 1e-300), "q": int(q)})
+        # Richardson pairs: the worst coordinates (normwise) and the BH mass at h / 2
+        worst = sorted(rows, key=lambda r: -r["err_normwise"])[:richardson]
+        for r in worst:
+            if time.monotonic() - t_leg + 2 * per_loss > allowance:
+                break
+            fd2, _ = fd_coord(r["q"], h / 2)
+            r["fd_h2"] = float(fd2)
+            r["err_normwise_h2"] = abs(r["g"] - fd2) / gmax
+        fdm2 = fd_mass(h / 2) if time.monotonic() - t_leg + 2 * per_loss <= allowance else None
+    tops = [r for r in rows if r["kind"] == "top_abs_g"]
+    out["fd_check_fp64"] = {
+        "steps": fd_steps, "h": h, "coords": len(rows), "skipped_for_time": skipped, "max_abs_g": gmax,
+        "max_err_normwise": max(r["err_normwise"] for r in rows) if rows else None,
+        "median_err_normwise": float(np.median([r["err_normwise"] for r in rows])) if rows else None,
+        "max_err_rel_top_abs_g": max(r["err_rel"] for r in tops) if tops else None,
+        "median_err_rel_top_abs_g": float(np.median([r["err_rel"] for r in tops])) if tops else None,
+        "bh_mass": {"g": float(gm), "fd": float(fdm), "err_rel": float(abs(gm - fdm) / abs(fdm)),
+                    "fd_h2": None if fdm2 is None else float(fdm2),
+                    "err_rel_h2": None if fdm2 is None else float(abs(gm - fdm2) / abs(fdm2))},
+        "richardson": [{k: r[k] for k in ("var", "particle", "k", "g", "fd", "fd_h2", "err_normwise",
+                                          "err_normwise_h2") if k in r} for r in worst],
+        "loss_eval_s": per_loss}
+    out["seconds"] = time.monotonic() - t_leg
+    return out
 
 
-def run_long(args, nstars, precisions, nsteps_by_prec, label):
-    """Energy drift and step throughput of device-resident runs (one JSON line)."""
+# ---------------------------------------------------------------------------- configuration 2
+def long_run(nstars, precisions, nsteps, every, allowance, label):
+    """Device-resident runs of the Plummer + BH workload at nstars: step throughput and the energy
+    drift E(t)/E(0) - 1 every `every` steps (energies in FP64 for both modes), then the largest
+    gap between the drift curves.  Stops early (and says so) when the allowance would be
+    exceeded."""
     import pn_gb300 as pn
+    t_leg = time.monotonic()
     s = pn.config_plummer(nstars, SEED, BH_FRACTION)
-    eps = pn.plummer_eps(nstars)
+    eps = plummer_eps(nstars)
     n = nstars + 1
     res = {}
     for prec in precisions:
         with pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=0) as c:
             c.set_state(s.x, s.v, s.m)
-            e0 = c.energy()[3]  # energies in FP64 for both modes
-            k = nsteps_by_prec[prec]
-            chunks = [k // 5 + (1 if q < k % 5 else 0) for q in range(5)]
-            ms, curve, done = [], [], 0
+            e0 = c.energy()[3]
+            ms, curve, done, truncated = [], [(0, 0.0)], 0, False
             with ClockSampler() as clk:
-                for kc in chunks:
-                    if kc == 0:
-                        continue
+                while done < nsteps:
+                    kc = min(every, nsteps - done)
+                    if ms:
+                        per = float(np.concatenate(ms).mean()) * 1e-3
+                        if time.monotonic() - t_leg + kc * per * 1.05 + 1.0 > allowance:
+                            truncated = True
+                            break
                     c.set_params(precision=prec)
                     ms.append(c.bench_steps(kc, flush_l2=False)[0])
                     done += kc
                     c.set_params(precision=0)
                     curve.append((done, float(c.energy()[3] / e0 - 1)))
-            ms = np.concatenate(ms)
+            allm = np.concatenate(ms)
             res["mixed" if prec else "fp64"] = {
-                "steps": k, "ms_per_step": float(ms.mean()), "value": 3.0 * n * n / (ms.mean() * 1e-3),
-                "energy_drift": curve[-1][1], "drift_curve": curve, "clocks": clk.summary()}
-    line = {"metric": label, "unit": UNIT, "n_gpus": 1, "data": "synthetic",
-            "config": dict(workload_config(nstars), dt=DT), **res}
-    print(json.dumps(line), flush=True)
-    return 0
+                "steps": done, "truncated": truncated, "ms_per_step": float(allm.mean()),
+                "value": 3.0 * n * n / (allm.mean() * 1e-3), "energy_drift": curve[-1][1],
+                "drift_curve": curve, "clocks": clk.summary()}
+    out = {"metric": label, "unit": UNIT, "config": dict(workload_config(nstars), steps=nsteps)}
+    out.update(res)
+    if "mixed" in res and "fp64" in res:
+        a = dict(res["mixed"]["drift_curve"])
+        b = dict(res["fp64"]["drift_curve"])
+        common = sorted(set(a) & set(b))
+        out["drift_max_abs_diff"] = max(abs(a[t] - b[t]) for t in common)
+        out["mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
+    out["seconds"] = time.monotonic() - t_leg
+    return out
 
 
 def profile_case(nstars, shape=None):
@@ -407,7 +512,7 @@ def profile_case(nstars, shape=None):
     if shape:
         ipt, tj, gs = (int(t) for t in shape.split(","))
         kw = dict(i_per_thread=ipt, tile_j=tj, grid_split=gs, pair_variant=2)
-    with pn.Context(nstars + 1, eps=pn.plummer_eps(nstars), inv_c2=INV_C2,
+    with pn.Context(nstars + 1, eps=plummer_eps(nstars), inv_c2=INV_C2,
                     precision=pn.PN_PREC_MIXED, **kw) as c:
         c.set_state(sysm.x, sysm.v, sysm.m)
         c.force()
@@ -436,50 +541,10 @@ def host_stage_step(pn, x, v, m, eps, dt):
     return (x + x3 + 2.0 * h) / 6.0, (v + v3 + 2.0 * hv) / 6.0
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=8)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="pn", choices=["pn", "reference"])
-    ap.add_argument("--nstars", type=int, default=NSTARS)
-    ap.add_argument("--quick", action="store_true", help="skip the FP64, accuracy and CPU legs")
-    ap.add_argument("--profile-case", type=int, default=0, metavar="N",
-                    help="set up N stars, tune, run one mixed force evaluation and exit (for ncu)")
-    ap.add_argument("--ensemble", action="store_true", help="configuration 4 (ensemble) instead")
-    ap.add_argument("--clusters", type=int, default=256)
-    ap.add_argument("--adjoint", action="store_true", help="configuration 5 (adjoint) instead")
-    ap.add_argument("--adj-n", type=int, default=16384)
-    ap.add_argument("--adj-steps", type=int, default=200)
-    ap.add_argument("--fd-coords", type=int, default=8)
-    ap.add_argument("--fd-steps", type=int, default=40)
-    ap.add_argument("--shape", default=None, help="--profile-case launch shape: ipt,tile_j,grid_split")
-    ap.add_argument("--fp64-run", type=int, default=0, metavar="STEPS",
-                    help="Plummer run at N=65536, FP64 and mixed, STEPS steps each (throughput, energy drift)")
-    ap.add_argument("--drift", type=int, default=0, metavar="STEPS",
-                    help="energy drift of the headline workload, mixed and FP64, STEPS steps each")
-    ap.add_argument("--long-mixed", type=int, default=0, metavar="STEPS",
-                    help="energy drift of the headline workload in mixed precision over STEPS steps")
-    args = ap.parse_args()
-    if args.fp64_run:
-        return run_long(args, 65536, (0, 1), {0: args.fp64_run, 1: args.fp64_run},
-                        "integration at N=65536, FP64 and mixed (interactions/s, energy drift)")
-    if args.drift:
-        return run_long(args, args.nstars, (1, 0), {1: args.drift, 0: args.drift},
-                        "energy drift, mixed vs FP64 (interactions/s per mode)")
-    if args.long_mixed:
-        return run_long(args, args.nstars, (1,), {1: args.long_mixed},
-                        "energy drift of the mixed-precision integration (interactions/s)")
-    if args.profile_case:
-        return profile_case(args.profile_case, args.shape)
-    if args.ensemble:
-        return run_ensemble(args)
-    if args.adjoint:
-        return run_adjoint(args)
-    rank, world, dist = dist_init(args.gpus)
-    if args.impl == "reference":
-        return run_reference(args, rank, world, dist)
-
+# ---------------------------------------------------------------------------- headline
+def headline(args, rank, world, dist):
+    """Configuration 3 (the metric's workload): the line's value, roofline, e2e, FP64, accuracy
+    and CPU baseline."""
     import pn_gb300 as pn
     from pn_gb300 import build as b
     if not os.path.exists(pn.LIB_PATH):
@@ -487,8 +552,7 @@ def main():
     ns = args.nstars
     n = ns + 1
     sysm = pn.config_plummer(ns, SEED + rank, BH_FRACTION)
-    eps = pn.plummer_eps(ns)
-    out = {}
+    eps = plummer_eps(ns)
 
     # ---------------- mixed precision, device resident (value)
     ctx = pn.Context(n, eps=eps, dt=DT, inv_c2=INV_C2, precision=pn.PN_PREC_MIXED)
@@ -497,9 +561,7 @@ def main():
     ctx.bench_steps(args.warmup, flush_l2=True)
     barrier(dist)
     with ClockSampler() as clk:
-        t0 = time.perf_counter()
         step_ms, pair_ms = ctx.bench_steps(args.steps, flush_l2=True)
-        wall = time.perf_counter() - t0
     barrier(dist)
     st = ctx.stats()
     total_ms = max_over_ranks(float(step_ms.sum()), dist)
@@ -513,12 +575,11 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded Plummer sphere + BH)",
-            "config": dict(workload_config(ns), parallelism=f"replicas{world}" if world > 1 else "1 GPU",
-                           pair_kernel={"tile_j": st.tile_j, "i_per_thread": st.i_per_thread,
-                                        "j_split": st.j_split, "grid_split": st.grid_split,
-                                        "threads": st.threads}),
+            "config": workload_config(ns, world),
             "gpu_launches": 9 * args.steps,
             "clocks": clk.summary(int(os.environ.get("LOCAL_RANK", "0")))}
+    launch_shape = {"tile_j": st.tile_j, "i_per_thread": st.i_per_thread, "j_split": st.j_split,
+                    "grid_split": st.grid_split, "threads": st.threads, "pair_variant": st.pair_variant}
 
     # roofline of the pair sweep against the measured FP32 FMA peak
     if rank == 0:
@@ -530,7 +591,7 @@ def main():
         line["roofline"] = {"bound": "fp32", "kernel": kname,
                             "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                             "frac": achieved / peak32, "traffic": None,
-                            "flops_per_pair": flops_pair,
+                            "flops_per_pair": flops_pair, "launch_shape": launch_shape,
                             "pair_launch_ms": pair_launch_ms,
                             "peak_source": "measured FP32 FMA throughput of this GPU (pn_probe_fma_peak)",
                             "pair_interactions_per_s": pairs / (pair_launch_ms * 1e-3)}
@@ -539,7 +600,9 @@ def main():
             try:  # DRAM bytes of one launch at this size and shape, from an ncu capture
                 pt = json.load(open(prof))
                 line["roofline"]["traffic"] = pt.get("k_pair2_force_f32_N262144_bytes_per_launch")
-                line["roofline"]["traffic_shape"] = pt.get("k_pair2_force_f32_N262144_shape")
+                line["roofline"]["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                                      "launch, committed profile (not this run): "
+                                                      + str(pt.get("k_pair2_force_f32_N262144_shape")))
                 line["roofline"]["ncu_fma_pipe_active_pct"] = pt.get("fma_pipe_active_pct_N65536")
             except (OSError, ValueError):
                 pass
@@ -606,12 +669,86 @@ def main():
                 "rms_abs_over_rms_a": float(np.sqrt((d ** 2).mean() / (np.linalg.norm(ref, axis=1) ** 2).mean()))}
         line["accuracy_vs_fp64"] = acc
         # ---------------- CPU baseline (oracle port), bounded sample
-        rate, info = cpu_baseline(sysm, eps)
-        rate1, info1 = cpu_baseline(sysm, eps, seconds=4.0, threads=1)  # the reference runs on one core
+        rate, info = cpu_baseline(sysm.x, sysm.v, sysm.m, eps)
+        rate1, info1 = cpu_baseline(sysm.x, sysm.v, sysm.m, eps, seconds=4.0, threads=1)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": info["threads"], "kind": "port",
                                 "sample": info["sample"], "seconds": info["seconds"],
                                 "single_core_value": rate1, "single_core_sample": info1["sample"]}
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="pn", choices=["pn", "reference"])
+    ap.add_argument("--nstars", type=int, default=NSTARS)
+    ap.add_argument("--quick", action="store_true",
+                    help="headline only: skip the FP64, accuracy, CPU and other-configuration legs")
+    ap.add_argument("--no-configs", action="store_true", help="skip the config2/4/5 legs of the line")
+    ap.add_argument("--budget-s", type=float, default=1500.0,
+                    help="wall-clock budget of the whole command; the config legs fit inside it")
+    ap.add_argument("--profile-case", type=int, default=0, metavar="N",
+                    help="set up N stars, tune, run one mixed force evaluation and exit (for ncu)")
+    ap.add_argument("--ensemble", action="store_true", help="configuration 4 (ensemble) alone")
+    ap.add_argument("--clusters", type=int, default=256)
+    ap.add_argument("--adjoint", action="store_true", help="configuration 5 (adjoint) alone")
+    ap.add_argument("--adj-n", type=int, default=16384)
+    ap.add_argument("--adj-steps", type=int, default=200)
+    ap.add_argument("--fd-coords", type=int, default=64)
+    ap.add_argument("--fd-steps", type=int, default=40)
+    ap.add_argument("--shape", default=None, help="--profile-case launch shape: ipt,tile_j,grid_split")
+    ap.add_argument("--fp64-run", type=int, default=0, metavar="STEPS",
+                    help="configuration 2 alone: N=65536, FP64 and mixed, STEPS steps each")
+    ap.add_argument("--drift", type=int, default=0, metavar="STEPS",
+                    help="energy drift of the headline workload, mixed and FP64, STEPS steps each")
+    ap.add_argument("--long-mixed", type=int, default=0, metavar="STEPS",
+                    help="energy drift of the headline workload in mixed precision over STEPS steps")
+    args = ap.parse_args()
+    budget = Budget(args.budget_s)
+    if args.impl == "reference":
+        # the reference arm is CPU work on rank 0 only: no process group, no GPU library
+        return run_reference(args, int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")))
+    if args.fp64_run:
+        every = max(1, args.fp64_run // 10)
+        r = long_run(65536, (1, 0), args.fp64_run, every, budget.left() - 30,
+                     "integration at N=65536, FP64 and mixed (interactions/s, energy drift)")
+        print(json.dumps(r), flush=True)
+        return 0
+    if args.drift:
+        r = long_run(args.nstars, (1, 0), args.drift, max(1, args.drift // 5), budget.left() - 30,
+                     "energy drift, mixed vs FP64 (interactions/s per mode)")
+        print(json.dumps(r), flush=True)
+        return 0
+    if args.long_mixed:
+        r = long_run(args.nstars, (1,), args.long_mixed, max(1, args.long_mixed // 5), budget.left() - 30,
+                     "energy drift of the mixed-precision integration (interactions/s)")
+        print(json.dumps(r), flush=True)
+        return 0
+    if args.profile_case:
+        return profile_case(args.profile_case, args.shape)
+    if args.ensemble:
+        print(json.dumps(ensemble_leg(args.steps, args.warmup, args.clusters, budget.left() - 30)), flush=True)
+        return 0
+    if args.adjoint:
+        print(json.dumps(adjoint_leg(args.adj_n, args.adj_steps, args.fd_steps, args.fd_coords,
+                                     budget.left() - 30)), flush=True)
+        return 0
+    rank, world, dist = dist_init(args.gpus)
+    line = headline(args, rank, world, dist)
+    if rank == 0 and world == 1 and not args.quick and not args.no_configs:
+        # the other configurations of the workload set, inside the remaining budget: config 2's
+        # FP64 run is the longest and goes last, keeping what the earlier legs leave
+        reserve = 30.0
+        line["config4"] = ensemble_leg(args.steps, args.warmup, 256, min(240.0, budget.left() - reserve - 1000))
+        line["config5"] = adjoint_leg(16384, 200, 40, 64, min(720.0, budget.left() - reserve - 640))
+        line["config2"] = long_run(65536, (1, 0), 500, 50, budget.left() - reserve,
+                                   "integration at N=65536 over 500 steps, FP64 and mixed "
+                                   "(interactions/s, energy drift)")
+        line["gpu_launches"] += line["config4"]["gpu_launches"]
     if rank == 0:
+        line["wall_s"] = time.monotonic() - T_START
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

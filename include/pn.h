@@ -201,14 +201,21 @@ int pn_selftest_wait_timeout(pn_ctx *ctx, double seconds);
  * asynchronous on it.  All work buffers live in one fixed device array of
  * PN_NOALLOC_SCRATCH_BYTES inside the library, held by every GPU that loads it until the
  * process exits, so n may not exceed PN_NOALLOC_NMAX (PN_ERR_INVALID otherwise).  The first call
- * on a device looks up that array's device address (make it before any stream capture).  Calls
- * share the array: calls that overlap on the GPU race.  Device-side problems (a non-finite
- * force) are not reported back; they show in d_a. */
+ * on a device looks up that array's device address and the device's SM count (make it before
+ * any stream capture).  Calls share the array: calls that overlap on the GPU race.  The return
+ * value covers the host-side checks and the launches; what only the GPU can see (a non-finite
+ * force, e.g. a star exactly on the BH; an in-kernel wait that gave up) is recorded in the
+ * array's error word and read back by pn_noalloc_status. */
 #define PN_NOALLOC_NMAX 8192
 #define PN_NOALLOC_SCRATCH_BYTES 3355904
 int pn_force_noalloc(int n, const double *d_x, const double *d_v, const double *d_m, double eps,
                      double inv_c2, int precision, double *d_a, void *stream);
+/* Host-side status of the calling thread's last pn_force_noalloc call. */
 int pn_noalloc_last_error(void);
+/* Device-side status of the last pn_force_noalloc call on the current device: waits for
+ * `stream` (the stream that call ran on), then copies the 4-byte error word into a host
+ * variable (no allocation).  PN_OK, PN_ERR_NONFINITE or PN_ERR_TIMEOUT. */
+int pn_noalloc_status(void *stream);
 
 /* ------------------------------------------------------------------ 2a. discrete adjoint */
 /* Vector-Jacobian product of one force evaluation at the current state: for abar (host AoS

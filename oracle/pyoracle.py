@@ -11,6 +11,10 @@ Two libraries live under ``oracle/``:
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import this
 module.  The product library never does.
+
+:func:`plummer_bh` samples the Plummer + BH workload with numpy alone (same construction as
+libpn's generator, its own random stream), so that the CPU arm of the benchmark builds its input
+without loading the GPU library.
 """
 from __future__ import annotations
 
@@ -42,9 +46,18 @@ def build(ref: bool = True) -> None:
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
 
 
+def reference_dir() -> str:
+    """The reference source tree: $LS9_DIR, else the Makefile's default (``make ls9-dir``)."""
+    d = os.environ.get("LS9_DIR")
+    if d:
+        return d
+    r = subprocess.run(["make", "-s", "-C", HERE, "ls9-dir"], capture_output=True, text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
+
+
 def reference_source_present() -> bool:
-    return os.path.exists(os.path.join(
-        os.environ.get("LS9_DIR", "/root/reference"), "Limit-sticky9.c"))
+    d = reference_dir()
+    return bool(d) and os.path.exists(os.path.join(d, "Limit-sticky9.c"))
 
 
 _lib = None
@@ -153,6 +166,50 @@ def _state(x, v, m):
     v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
     m = np.ascontiguousarray(m, dtype=np.float64).reshape(-1)
     assert x.shape == v.shape and x.shape[0] == m.shape[0]
+    return x, v, m
+
+
+def plummer_bh(nstars, seed=1, bh_fraction=0.01):
+    """A Plummer sphere of nstars equal-mass stars in Henon units (M = 1, E = -1/4) by the
+    Aarseth-Henon-Wielen (1974) method -- radius from the cumulative mass with the outer 0.1 %
+    cut, speed ratio q from g(q) = q^2 (1 - q^2)^(7/2) by rejection, isotropic directions,
+    centre-of-mass frame -- plus a BH of bh_fraction x the stellar mass at the origin at rest
+    (row 0).  numpy's generator, vectorised: the same distribution as libpn's pn_ic_plummer,
+    not the same random numbers.  Returns (x, v, m), AoS float64."""
+    rng = np.random.default_rng(seed)
+    n = int(nstars)
+
+    def iso(r):
+        z = (1.0 - 2.0 * rng.random(r.size)) * r
+        ph = 2.0 * np.pi * rng.random(r.size)
+        rho = np.sqrt(np.maximum(r * r - z * z, 0.0))
+        return np.stack([rho * np.cos(ph), rho * np.sin(ph), z], axis=1)
+
+    X1 = np.empty(n)
+    todo = np.arange(n)
+    while todo.size:
+        u = rng.random(todo.size)
+        ok = (u > 1e-12) & (u <= 0.999)
+        X1[todo[ok]] = u[ok]
+        todo = todo[~ok]
+    r = 1.0 / np.sqrt(X1 ** (-2.0 / 3.0) - 1.0)
+    q = np.empty(n)
+    todo = np.arange(n)
+    while todo.size:
+        X4, X5 = rng.random(todo.size), rng.random(todo.size)
+        ok = 0.1 * X5 < X4 * X4 * (1.0 - X4 * X4) ** 3.5
+        q[todo[ok]] = X4[ok]
+        todo = todo[~ok]
+    rscale = 3.0 * np.pi / 16.0
+    xs = iso(r) * rscale
+    vs = iso(q * np.sqrt(2.0) * (1.0 + r * r) ** -0.25) / np.sqrt(rscale)
+    xs -= xs.mean(axis=0)
+    vs -= vs.mean(axis=0)
+    x = np.zeros((n + 1, 3))
+    v = np.zeros((n + 1, 3))
+    x[1:], v[1:] = xs, vs
+    m = np.full(n + 1, 1.0 / max(n, 1))
+    m[0] = bh_fraction
     return x, v, m
 
 

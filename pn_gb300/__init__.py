@@ -107,6 +107,7 @@ SIGNATURES = [
                                         ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_void_p,
                                         ctypes.c_void_p]),
     ("pn_noalloc_last_error", ctypes.c_int, []),
+    ("pn_noalloc_status", ctypes.c_int, [ctypes.c_void_p]),
     ("pn_force_vjp", ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
     ("pn_adj_forward", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     ("pn_adj_backward", ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp]),

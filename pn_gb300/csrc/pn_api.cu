@@ -132,8 +132,8 @@ static PairCfg choose_cfg(const pn_ctx *c, int mode, int nstar) {
     const int bi = pair_block_i(k);
     const int nib = (nstar + bi - 1) / bi;
     const int ntiles = (nstar + k.tj - 1) / k.tj;
-    // j-splits for about 8 waves of 4 CTAs on 152 SMs, keeping >= 4 tiles per split
-    int g = c->p.grid_split > 0 ? c->p.grid_split : (8 * 152 * 4 + nib - 1) / (nib > 0 ? nib : 1);
+    // j-splits for about 8 waves of 4 CTAs per SM, keeping >= 4 tiles per split
+    int g = c->p.grid_split > 0 ? c->p.grid_split : (8 * c->sms * 4 + nib - 1) / (nib > 0 ? nib : 1);
     if (c->p.grid_split <= 0) {
         if (g > 32) g = 32;
         if (g > ntiles / 4) g = ntiles / 4;
@@ -219,6 +219,12 @@ extern "C" int pn_create(pn_ctx **out, int nmax, const pn_params *p) {
     c->npad = (int)round_up(nmax > 1 ? nmax - 1 : 1, 256);
     c->ld = round_up(nmax, 256);
     cudaGetDevice(&c->dev);
+    if (cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->dev) != cudaSuccess || c->sms < 1) {
+        cudaGetLastError();
+        const int dev = c->dev;
+        delete c;
+        return set_err(PN_ERR_CUDA, "pn_create: SM count of device %d", dev);
+    }
     auto fail = [&](const char *what) {
         cudaGetLastError();
         free_ctx(c);

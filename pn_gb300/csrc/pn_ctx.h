@@ -9,6 +9,7 @@ struct AdjointWork;  // pn_adjoint.cu
 
 struct pn_ctx {
     int dev = 0;
+    int sms = 0;       // SM count of dev (launch-shape heuristics)
     int nmax = 0, n = 0;
     int npad = 0;      // padded star capacity (multiple of 256)
     long long ld = 0;  // state leading dimension

@@ -17,6 +17,16 @@
 // error word are cleared at the start of every call (cudaMemsetAsync on the caller's stream),
 // everything else is written before it is read.  Calls whose executions overlap on the GPU (on
 // different streams, or on one device from several host threads) race on the array.
+//
+// Device-side outcomes (a non-finite force, e.g. a star exactly on the BH; an in-kernel wait
+// that gave up) are recorded in the array's error word; pn_noalloc_status() waits for the
+// caller's stream and reads that word into a host variable (a plain device-to-host copy, no
+// allocation), so the caller learns them without allocating anything either.
+//
+// The per-device set-up (symbol address, SM count) is published through atomics: two host
+// threads making their first call on one device at the same time both look the values up and
+// store the same result, which is well defined.
+#include <atomic>
 #include <cstdio>
 
 #include "../../include/pn.h"
@@ -51,18 +61,23 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kBytes];
 
 namespace {
 constexpr int kMaxDevices = 64;
-unsigned char *g_dev_ptr[kMaxDevices] = {};  // device address of g_noalloc_scratch per device
+// per device: the device address of g_noalloc_scratch and the SM count (0 = not looked up yet)
+std::atomic<unsigned char *> g_dev_ptr[kMaxDevices];
+std::atomic<int> g_dev_sms[kMaxDevices];
 thread_local int g_noalloc_err = PN_OK;
 }  // namespace
 
-// Device address of the scratch array on the current device (set up on first use).
-static int scratch_address(unsigned char **out) {
+// Device address of the scratch array and the SM count of the current device (looked up on
+// the first call made on that device, with that device current).
+static int scratch_address(unsigned char **out, int *sms_out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         cudaGetLastError();
         return PN_ERR_UNSUPPORTED;
     }
-    if (!g_dev_ptr[dev]) {
+    unsigned char *ptr = g_dev_ptr[dev].load(std::memory_order_acquire);
+    int sms = g_dev_sms[dev].load(std::memory_order_acquire);
+    if (!ptr || sms <= 0) {
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
@@ -70,13 +85,38 @@ static int scratch_address(unsigned char **out) {
             cudaGetLastError();
             return PN_ERR_CUDA;
         }
-        g_dev_ptr[dev] = static_cast<unsigned char *>(p);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+            cudaGetLastError();
+            return PN_ERR_CUDA;
+        }
+        ptr = static_cast<unsigned char *>(p);
+        g_dev_sms[dev].store(sms, std::memory_order_release);
+        g_dev_ptr[dev].store(ptr, std::memory_order_release);
     }
-    *out = g_dev_ptr[dev];
+    *out = ptr;
+    if (sms_out) *sms_out = sms;
     return PN_OK;
 }
 
 extern "C" int pn_noalloc_last_error(void) { return g_noalloc_err; }
+
+extern "C" int pn_noalloc_status(void *stream) {
+    unsigned char *base = nullptr;
+    int rc = scratch_address(&base, nullptr);
+    if (rc) return rc;
+    if (cudaStreamSynchronize(static_cast<cudaStream_t>(stream)) != cudaSuccess) {
+        cudaGetLastError();
+        return PN_ERR_CUDA;
+    }
+    int word = 0;  // a host stack variable: the copy allocates nothing
+    if (cudaMemcpy(&word, base + kOffErr, sizeof word, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return PN_ERR_CUDA;
+    }
+    if (word & DEVERR_TIMEOUT) return PN_ERR_TIMEOUT;
+    if (word & DEVERR_NONFINITE) return PN_ERR_NONFINITE;
+    return PN_OK;
+}
 
 extern "C" int pn_force_noalloc(int n, const double *d_x, const double *d_v, const double *d_m,
                                 double eps, double inv_c2, int precision, double *d_a, void *stream) {
@@ -92,7 +132,8 @@ extern "C" int pn_force_noalloc(int n, const double *d_x, const double *d_v, con
         (precision != PN_PREC_FP64 && precision != PN_PREC_MIXED))
         return fail(PN_ERR_INVALID);
     unsigned char *base = nullptr;
-    int rc = scratch_address(&base);
+    int sms = 0;
+    int rc = scratch_address(&base, &sms);
     if (rc) return fail(rc);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     double *spos = reinterpret_cast<double *>(base + kOffSpos);
@@ -118,7 +159,7 @@ extern "C" int pn_force_noalloc(int n, const double *d_x, const double *d_v, con
     const int bi = PAIR_NT * k.ipt;
     const int nib = (nstar + bi - 1) / bi;
     const int ntiles = (nstar + k.tj - 1) / k.tj;
-    int g = nib > 0 ? (4 * 152 * 4 + nib - 1) / nib : 1;
+    int g = nib > 0 ? (4 * sms * 4 + nib - 1) / nib : 1;  // about 4 waves of 4 CTAs per SM
     if (g > kMaxSplits) g = kMaxSplits;
     if (g > ntiles) g = ntiles;
     if (g < 1) g = 1;

@@ -3,8 +3,8 @@
 The reference functions (Limit-sticky9.c force / initial_energy, and its integration step)
 are compiled from their own source by ``oracle/Makefile`` (target ``ref``) into
 ``oracle/_ref/libls9ref.so``; this script calls them through ``oracle/pyoracle.py``.  It needs
-the reference source tree (``LS9_DIR``, default /root/reference) and only runs where that
-exists; the .npz files it writes are committed, so the tests do not need the reference.
+the reference source tree (``LS9_DIR``, else the default of ``oracle/Makefile``) and only runs
+where that exists; the .npz files it writes are committed, so the tests do not need the reference.
 
     python tests/golden/make_golden.py [case ...]      (cases: kat random init10k config1)
 
@@ -86,7 +86,7 @@ def case_random():
 
 
 def case_init10k():
-    src = os.path.join(os.environ.get("LS9_DIR", "/root/reference"), "Init10k-sphere.dat")
+    src = os.path.join(po.reference_dir(), "Init10k-sphere.dat")
     nstars = 2000
     xs = np.zeros((nstars, 3))
     with open(src) as fh:

@@ -107,3 +107,48 @@ def test_ensemble_explicit_shapes(pn, oracle):
             acc = e.force()
         for s, a, ep in zip(systems, acc, eps):
             assert fp64_close(a, oracle.force_exact(s.x, s.v, s.m, ep))
+
+
+def test_ensemble_256_clusters_persistent_queue(pn, oracle):
+    """The ensemble configuration's shape at test size: 256 Plummer + BH clusters, N log-uniform
+    in [64, 2048], BH mass fraction log-uniform in [1e-3, 1e-1], eps = 0.01, dt = 1/1024, so the
+    persistent queue runs at the real item count.  Every cluster of the FP64 ensemble equals its
+    individual FP64 run (1e-12) and every cluster of the tuned mixed ensemble stays close to it
+    after 10 steps (positions 1e-8, velocities 1e-6 of the largest); a few clusters' forces at c = 1 are checked against the exact oracle."""
+    rng = np.random.default_rng(256)
+    nc = 256
+    sizes = np.exp(rng.uniform(np.log(64), np.log(2048), nc)).astype(int)
+    fracs = np.exp(rng.uniform(np.log(1e-3), np.log(1e-1), nc))
+    systems = [pn.config_plummer(int(s), 5000 + k, float(f)) for k, (s, f) in enumerate(zip(sizes, fracs))]
+    eps = [0.01] * nc
+    nsteps = 10
+    states = {}
+    for prec in (0, 1):
+        with pn.Ensemble(systems, eps, precision=prec, dt=1 / 1024, inv_c2=1e-6) as e:
+            if prec == 1:
+                e.autotune()
+            e.steps(nsteps)
+            states[prec] = e.get_state()
+    for k, s in enumerate(systems):
+        with pn.Context(s.x.shape[0], eps=eps[k], dt=1 / 1024, inv_c2=1e-6) as c:
+            c.set_state(s.x, s.v, s.m)
+            c.steps(nsteps)
+            xr, vr = c.get_state()
+        x64, v64 = states[0][0][k], states[0][1][k]
+        x32, v32 = states[1][0][k], states[1][1][k]
+        assert np.abs(x64 - xr).max() <= 1e-12 * np.abs(xr).max(), k
+        assert np.abs(v64 - vr).max() <= 1e-12 * np.abs(vr).max(), k
+        # mixed: FP32 pair terms (per-particle force error ~1e-6 at worst) over 30 evaluations
+        assert np.abs(x32 - xr).max() <= 1e-8 * np.abs(xr).max(), k
+        assert np.abs(v32 - vr).max() <= 1e-6 * np.abs(vr).max(), k
+    picks = sorted({int(np.argmin(sizes)), int(np.argmax(sizes))} | {int(q) for q in rng.choice(nc, 3, replace=False)})
+    forces = {}
+    for prec in (0, 1):
+        with pn.Ensemble(systems, eps, precision=prec, inv_c2=1.0) as e:
+            forces[prec] = e.force()
+    for k in picks:
+        s = systems[k]
+        ax = oracle.force_exact(s.x, s.v, s.m, eps[k])
+        assert fp64_close(forces[0][k], ax), k
+        d = np.linalg.norm(forces[1][k] - ax, axis=1)
+        assert np.sqrt((d ** 2).mean() / (np.linalg.norm(ax, axis=1) ** 2).mean()) <= 1e-6, k

@@ -1,15 +1,16 @@
-"""The integration recipe of INTEGRATION.md section 2, checked on the CPU: a temporary copy of
-the reference's Limit-sticky9.c with the PN_GPU guard compiles with gcc and its main loop links
-against libpn's drop-in entry points (run only where the reference source is present; the
-binary is not run -- it needs a GPU and integrates to t = 10)."""
+"""The drop-in integration recipe, checked on the CPU: a temporary copy of the reference's
+Limit-sticky9.c with a PN_GPU guard around its own force/energy functions compiles with gcc and
+its main loop links against libpn's drop-in entry points (run only where the reference source
+is present; the linked binary itself runs on the GPU in test_reference_main_gpu.py)."""
 import os
 import subprocess
 
 import pytest
 
 from conftest import ROOT
+from oracle import pyoracle
 
-LS9 = os.path.join(os.environ.get("LS9_DIR", "/root/reference"), "Limit-sticky9.c")
+LS9 = os.path.join(pyoracle.reference_dir(), "Limit-sticky9.c")
 
 
 @pytest.mark.skipif(not os.path.exists(LS9), reason="reference source not present")
