@@ -207,7 +207,7 @@ int pn_selftest_wait_timeout(pn_ctx *ctx, double seconds);
  * force, e.g. a star exactly on the BH; an in-kernel wait that gave up) is recorded in the
  * array's error word and read back by pn_noalloc_status. */
 #define PN_NOALLOC_NMAX 8192
-#define PN_NOALLOC_SCRATCH_BYTES 3355904
+#define PN_NOALLOC_SCRATCH_BYTES 3364096
 int pn_force_noalloc(int n, const double *d_x, const double *d_v, const double *d_m, double eps,
                      double inv_c2, int precision, double *d_a, void *stream);
 /* Host-side status of the calling thread's last pn_force_noalloc call. */

@@ -24,6 +24,7 @@
 // stage adjoints, with one force VJP per stage).
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -204,9 +205,21 @@ enum VjpRowSum : int {
 // LQ = 3 m Q^2 (gd + S0bar + br wd + k4 wdv) + Phibar m + Ubar mu3 + wd (3 mQ^3 vdj^2 Q + k35).
 // The self pair (q = p, d = 0) contributes only Ubar_p / eps to mu3bar; it is skipped here
 // (Q = 0) and that term is added per row, so no 1/eps^3 term has to cancel in the sums.
+// The intermediates of the two pair terms of one unordered pair {p, q}: F(p, q) with p's adjoint
+// state (role 1 of row p, role 2 of row q) and F(q, p) with q's adjoint state (role 2 of row p,
+// role 1 of row q).  d = s_q - s_p.
+template <typename T> struct VjpTerms {
+    T Q, rp, rq;               // inverse distance (0 for the self pair); rhoe - qe_p, rhoe - qe_q
+    T mQ3, ga, h, cd, cv, be;  // F(p, q): m_q Q^3, mQ^3 wd, mQ^3 wdv, cd, cv, beta
+    T mQ3b, ga2, h2, cd2, cv2, be2;  // F(q, p), the same quantities
+    T wd, wq;                  // Wbar_p . d, Wbar_q . d
+    T cS, cSv, cV, cVd;        // coefficients of the shared vector sums
+};
+
 template <typename T>
-__device__ __forceinline__ void vjp_pair(T *y, const VjpState<T> &P, const VjpState<T> &Qj, T dx, T dy,
-                                         T dz, T eps2, bool self) {
+__device__ __forceinline__ VjpTerms<T> vjp_terms(const VjpState<T> &P, const VjpState<T> &Qj, T dx, T dy, T dz,
+                                                 T eps2, bool self) {
+    VjpTerms<T> r;
     const T rhoe = pn_fma(dz, dz, pn_fma(dy, dy, pn_fma(dx, dx, eps2)));
     T Q = pn_rsqrt<T>(rhoe);
     if (self) Q = T(0);
@@ -215,13 +228,14 @@ __device__ __forceinline__ void vjp_pair(T *y, const VjpState<T> &P, const VjpSt
     const T vdq = pn_fma(Qj.vz, dz, pn_fma(Qj.vy, dy, Qj.vx * dx));  // v_q . d
     const T vpq = pn_fma(P.vz, Qj.vz, pn_fma(P.vy, Qj.vy, P.vx * Qj.vx));
     const T dv2 = pn_fma(T(-2), vpq, P.vi2 + Qj.vi2);               // |v_q - v_p|^2
-    // ---- role 1: (i, j) = (p, q), adjoint state of p
+    // ---- F(p, q): (i, j) = (p, q), adjoint state of p
     const T mQ3 = Qj.m * Q3;
     const T gd = pn_fma(P.Gz, dz, pn_fma(P.Gy, dy, P.Gx * dx));
     const T wd = pn_fma(P.Wz, dz, pn_fma(P.Wy, dy, P.Wx * dx));
     const T wdv = pn_fma(P.Wz, Qj.vz, pn_fma(P.Wy, Qj.vy, pn_fma(P.Wx, Qj.vx, -P.cW)));
     const T t = vdq * vdq;
-    T br = pn_fma(rhoe - P.qe, Qj.c3, Qj.c1) + pn_fma(T(-2), dv2, P.vi2);
+    const T rp = rhoe - P.qe;
+    T br = pn_fma(rp, Qj.c3, Qj.c1) + pn_fma(T(-2), dv2, P.vi2);
     br = pn_fma(T(1.5) * t, Q2, br);
     const T k4 = pn_fma(T(4), vdp, T(-3) * vdq);
     const T cd = pn_fma(mQ3, br, Qj.k35 * Q);
@@ -233,13 +247,7 @@ __device__ __forceinline__ void vjp_pair(T *y, const VjpState<T> &P, const VjpSt
     const T h = mQ3 * wdv;
     const T al = pn_fma(T(2) * Qj.c3, ga, -LQ * Q3);
     const T be = T(3) * pn_fma(Q2 * vdq, ga, -h);
-    y[Y_A] += h;
-    y[Y_B] += cd;
-    y[Y_SG] += ga;
-    y[Y_SCV] += cv;
-    y[Y_QE] = pn_fma(Qj.c3, ga, y[Y_QE]);
-    y[Y_S0] += mQ3;
-    // ---- role 2: (i, j) = (q, p), adjoint state of q; d' = -d, dv' = v_p - v_q
+    // ---- F(q, p): (i, j) = (q, p), adjoint state of q; d' = -d, dv' = v_p - v_q
     const T mQ3b = P.m * Q3;
     const T gq = pn_fma(Qj.Gz, dz, pn_fma(Qj.Gy, dy, Qj.Gx * dx));  // -gd'
     const T wq = pn_fma(Qj.Wz, dz, pn_fma(Qj.Wy, dy, Qj.Wx * dx));  // -wd'
@@ -258,20 +266,76 @@ __device__ __forceinline__ void vjp_pair(T *y, const VjpState<T> &P, const VjpSt
     const T h2 = mQ3b * wdv2;
     const T al2 = pn_fma(T(2) * P.c3, ga2, -LQ2 * Q3);
     const T be2 = T(-3) * pn_fma(Q2 * vdp, ga2, h2);
-    y[Y_SG2] += ga2;
-    y[Y_SB2] += be2;
-    y[Y_MU3] = pn_fma(Qj.U, Q, y[Y_MU3]);
-    y[Y_C3] = pn_fma(ga2, rq, y[Y_C3]);
-    y[Y_K35] = pn_fma(-Q, wq, y[Y_K35]);
-    // ---- shared vector sums
-    const T cS = -(al + al2), cSv = pn_fma(T(4), h2, -be);
-    y[Y_SX] = pn_fma(cd2, Qj.Wx, pn_fma(mQ3b, Qj.Gx, pn_fma(cSv, Qj.vx, pn_fma(cS, dx, y[Y_SX]))));
-    y[Y_SY] = pn_fma(cd2, Qj.Wy, pn_fma(mQ3b, Qj.Gy, pn_fma(cSv, Qj.vy, pn_fma(cS, dy, y[Y_SY]))));
-    y[Y_SZ] = pn_fma(cd2, Qj.Wz, pn_fma(mQ3b, Qj.Gz, pn_fma(cSv, Qj.vz, pn_fma(cS, dz, y[Y_SZ]))));
-    const T cV = T(4) * (ga + ga2), cVd = pn_fma(T(4), h, -be2);
-    y[Y_VX] = pn_fma(cv2, Qj.Wx, pn_fma(cVd, dx, pn_fma(cV, Qj.vx, y[Y_VX])));
-    y[Y_VY] = pn_fma(cv2, Qj.Wy, pn_fma(cVd, dy, pn_fma(cV, Qj.vy, y[Y_VY])));
-    y[Y_VZ] = pn_fma(cv2, Qj.Wz, pn_fma(cVd, dz, pn_fma(cV, Qj.vz, y[Y_VZ])));
+    r.Q = Q; r.rp = rp; r.rq = rq;
+    r.mQ3 = mQ3; r.ga = ga; r.h = h; r.cd = cd; r.cv = cv; r.be = be;
+    r.mQ3b = mQ3b; r.ga2 = ga2; r.h2 = h2; r.cd2 = cd2; r.cv2 = cv2; r.be2 = be2;
+    r.wd = wd; r.wq = wq;
+    r.cS = -(al + al2);
+    r.cSv = pn_fma(T(4), h2, -be);
+    r.cV = T(4) * (ga + ga2);
+    r.cVd = pn_fma(T(4), h, -be2);
+    return r;
+}
+
+// Row p's sums from the pair terms: role 1 (F(p, q)) and role 2 (F(q, p)), shared vector sums.
+template <typename T>
+__device__ __forceinline__ void vjp_acc_p(T *y, const VjpTerms<T> &r, const VjpState<T> &Qj, T dx, T dy, T dz) {
+    y[Y_A] += r.h;
+    y[Y_B] += r.cd;
+    y[Y_SG] += r.ga;
+    y[Y_SCV] += r.cv;
+    y[Y_QE] = pn_fma(Qj.c3, r.ga, y[Y_QE]);
+    y[Y_S0] += r.mQ3;
+    y[Y_SG2] += r.ga2;
+    y[Y_SB2] += r.be2;
+    y[Y_MU3] = pn_fma(Qj.U, r.Q, y[Y_MU3]);
+    y[Y_C3] = pn_fma(r.ga2, r.rq, y[Y_C3]);
+    y[Y_K35] = pn_fma(-r.Q, r.wq, y[Y_K35]);
+    y[Y_SX] = pn_fma(r.cd2, Qj.Wx, pn_fma(r.mQ3b, Qj.Gx, pn_fma(r.cSv, Qj.vx, pn_fma(r.cS, dx, y[Y_SX]))));
+    y[Y_SY] = pn_fma(r.cd2, Qj.Wy, pn_fma(r.mQ3b, Qj.Gy, pn_fma(r.cSv, Qj.vy, pn_fma(r.cS, dy, y[Y_SY]))));
+    y[Y_SZ] = pn_fma(r.cd2, Qj.Wz, pn_fma(r.mQ3b, Qj.Gz, pn_fma(r.cSv, Qj.vz, pn_fma(r.cS, dz, y[Y_SZ]))));
+    y[Y_VX] = pn_fma(r.cv2, Qj.Wx, pn_fma(r.cVd, dx, pn_fma(r.cV, Qj.vx, y[Y_VX])));
+    y[Y_VY] = pn_fma(r.cv2, Qj.Wy, pn_fma(r.cVd, dy, pn_fma(r.cV, Qj.vy, y[Y_VY])));
+    y[Y_VZ] = pn_fma(r.cv2, Qj.Wz, pn_fma(r.cVd, dz, pn_fma(r.cV, Qj.vz, y[Y_VZ])));
+}
+
+// Row q's sums from the same terms: the roles exchange (F(q, p) is q's role 1, F(p, q) its
+// role 2) and d -> -d; the shared coefficients swap too (q's cSv is p's cVd and vice versa).
+template <typename T>
+__device__ __forceinline__ void vjp_acc_q(T *z, const VjpTerms<T> &r, const VjpState<T> &P, T dx, T dy, T dz) {
+    z[Y_A] += r.h2;
+    z[Y_B] += r.cd2;
+    z[Y_SG] += r.ga2;
+    z[Y_SCV] += r.cv2;
+    z[Y_QE] = pn_fma(P.c3, r.ga2, z[Y_QE]);
+    z[Y_S0] += r.mQ3b;
+    z[Y_SG2] += r.ga;
+    z[Y_SB2] += r.be;
+    z[Y_MU3] = pn_fma(P.U, r.Q, z[Y_MU3]);
+    z[Y_C3] = pn_fma(r.ga, r.rp, z[Y_C3]);
+    z[Y_K35] = pn_fma(r.Q, r.wd, z[Y_K35]);
+    z[Y_SX] = pn_fma(r.cd, P.Wx, pn_fma(r.mQ3, P.Gx, pn_fma(r.cVd, P.vx, pn_fma(-r.cS, dx, z[Y_SX]))));
+    z[Y_SY] = pn_fma(r.cd, P.Wy, pn_fma(r.mQ3, P.Gy, pn_fma(r.cVd, P.vy, pn_fma(-r.cS, dy, z[Y_SY]))));
+    z[Y_SZ] = pn_fma(r.cd, P.Wz, pn_fma(r.mQ3, P.Gz, pn_fma(r.cVd, P.vz, pn_fma(-r.cS, dz, z[Y_SZ]))));
+    z[Y_VX] = pn_fma(r.cv, P.Wx, pn_fma(-r.cSv, dx, pn_fma(r.cV, P.vx, z[Y_VX])));
+    z[Y_VY] = pn_fma(r.cv, P.Wy, pn_fma(-r.cSv, dy, pn_fma(r.cV, P.vy, z[Y_VY])));
+    z[Y_VZ] = pn_fma(r.cv, P.Wz, pn_fma(-r.cSv, dz, pn_fma(r.cV, P.vz, z[Y_VZ])));
+}
+
+// One (p, q) pair, both roles, into row p's sums (the ordered sweep).  The algebra: with
+// F = Gbar.(mQ^3 d) + Phibar mQ + S0bar mQ^3 + Ubar mu3 Q + Wbar.(cd d + cv dv) for one ordered
+// pair (i, j),
+//   dF/dd  = mQ^3 [Gbar + 2 c3 wd d + 3 Q^2 vdj wd v_j + wdv (4 v_i - 3 v_j)] + cd Wbar - LQ Q^3 d
+//   dF/dv_i = mQ^3 wd (4 v_j - 2 v_i) + 4 mQ^3 wdv d - cv Wbar
+//   dF/dv_j = mQ^3 wd (4 (v_i - v_j) - 3 Q^2 vdj d) ... + cv Wbar   (role 2, with d -> -d)
+// LQ = 3 m Q^2 (gd + S0bar + br wd + k4 wdv) + Phibar m + Ubar mu3 + wd (3 mQ^3 vdj^2 Q + k35).
+// The self pair (q = p, d = 0) contributes only Ubar_p / eps to mu3bar; it is skipped here
+// (Q = 0) and that term is added per row, so no 1/eps^3 term has to cancel in the sums.
+template <typename T>
+__device__ __forceinline__ void vjp_pair(T *y, const VjpState<T> &P, const VjpState<T> &Qj, T dx, T dy,
+                                         T dz, T eps2, bool self) {
+    const VjpTerms<T> r = vjp_terms<T>(P, Qj, dx, dy, dz, eps2, self);
+    vjp_acc_p<T>(y, r, Qj, dx, dy, dz);
 }
 
 // The row's outputs (NV_VJP slots) from its sums, in FP64.  qself = 1/eps for the split whose
@@ -429,6 +493,130 @@ __global__ void __launch_bounds__(VJP_NT) k_pair_vjp(const PairVjpArgs a) {
     }
 }
 
+// ------------------------------------------------------------------ the symmetric adjoint sweep
+// Each unordered pair {p, q} is visited once: the intermediates of its two pair terms serve both
+// rows (vjp_acc_p, vjp_acc_q), about 94 operations per ordered pair instead of 154.
+//
+// Work item = a pair of 128-star tiles (I, J), I <= J (the pack's tiles), one CTA of four warps.
+// Tile J is staged in shared memory; warp w holds the rows p of stars I*128 + 32w + lane in
+// registers.  For each 32-star sub-tile k of J, lane l visits q = 32k + (l + s) mod 32 at step s,
+// so the 32 lanes meet 32 different q, and the running sums of row q travel with q: after each
+// step every lane passes its q-sums to lane l - 1 (one shuffle per sum).  After 32 steps lane l
+// holds the warp's sums for q = 32k + l; the four warps' sums are added in a fixed order in
+// shared memory.  The CTA writes row p's sums from tile J to part[J][.][p] and row q's sums from
+// tile I to part[I][.][q]: every (tile, star) slot of part is written by exactly one CTA, and
+// k_vjp_sym_rows adds a star's slots in tile order in FP64 (deterministic).  A diagonal item
+// (I = J) visits every pair of its tile in both orders, so its sums are halved; the self pair is
+// skipped (its mu3 term is added per row, as in the ordered sweep).
+constexpr int SYM_T = 128;
+
+template <typename T> constexpr int sym_min_blocks() { return sizeof(T) == 4 ? 4 : 2; }
+
+template <typename T>
+constexpr size_t sym_smem_bytes() {
+    return (size_t)(VjpPack<T>::NGF + VjpPack<T>::NGA) * SYM_T * sizeof(typename VjpPack<T>::V) +
+           (size_t)4 * NY * SYM_T * sizeof(T);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SYM_T, (sym_min_blocks<T>())) k_pair_vjp_sym(const PairVjpArgs a, T *part) {
+    using V = typename VjpPack<T>::V;
+    constexpr int NGF = VjpPack<T>::NGF, NGA = VjpPack<T>::NGA;
+    constexpr bool F32 = sizeof(T) == 4;
+    extern __shared__ __align__(128) unsigned char smem[];
+    V *qd = reinterpret_cast<V *>(smem);                                          // [NGF + NGA][SYM_T]
+    T *qp = reinterpret_cast<T *>(smem + (size_t)(NGF + NGA) * SYM_T * sizeof(V));  // [4][NY][SYM_T]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // work item u -> tile pair (I, J), I <= J, u = J (J + 1) / 2 + I
+    const long long u = blockIdx.x;
+    int J = (int)((sqrt(8.0 * (double)u + 1.0) - 1.0) * 0.5);
+    while ((long long)J * (J + 1) / 2 > u) --J;
+    while ((long long)(J + 1) * (J + 2) / 2 <= u) ++J;
+    const int I = (int)(u - (long long)J * (J + 1) / 2);
+    const bool diag = I == J;
+    const V *pf = static_cast<const V *>(a.pack);
+    const V *pa = static_cast<const V *>(a.apack);
+    const int q0 = J * SYM_T;
+#pragma unroll
+    for (int g = 0; g < NGF; ++g) qd[g * SYM_T + tid] = pf[(size_t)g * a.npad + q0 + tid];
+#pragma unroll
+    for (int g = 0; g < NGA; ++g) qd[(NGF + g) * SYM_T + tid] = pa[(size_t)g * a.npad + q0 + tid];
+    const int p = I * SYM_T + tid;
+    VjpState<T> P;
+    vjp_load<T>(P, pf, pa, a.npad, p);
+    if constexpr (F32) {  // p relative to tile J's origin, as an FP32 hi/lo pair
+        const TileOrigin o = a.torg[J];
+        const double rx = a.spos[p] - o.x, ry = a.spos[a.npad + p] - o.y, rz = a.spos[2 * a.npad + p] - o.z;
+        P.ex = (float)rx; P.ey = (float)ry; P.ez = (float)rz;
+        P.lx = (float)(rx - (double)P.ex); P.ly = (float)(ry - (double)P.ey); P.lz = (float)(rz - (double)P.ez);
+    }
+    T y[NY], z[NY];
+#pragma unroll
+    for (int c = 0; c < NY; ++c) y[c] = T(0);
+    __syncthreads();
+    const T eps2 = (T)a.eps2;
+    const V *qa = qd + NGF * SYM_T;
+    const int from = (lane + 1) & 31;
+    for (int k = 0; k < SYM_T / 32; ++k) {
+#pragma unroll
+        for (int c = 0; c < NY; ++c) z[c] = T(0);
+#pragma unroll 1
+        for (int st = 0; st < 32; ++st) {
+            const int qi = k * 32 + ((lane + st) & 31);
+            VjpState<T> Qj;
+            vjp_load<T>(Qj, qd, qa, SYM_T, qi);
+            T dx, dy, dz;
+            if constexpr (F32) {
+                dx = (Qj.ex - P.ex) + (Qj.lx - P.lx);
+                dy = (Qj.ey - P.ey) + (Qj.ly - P.ly);
+                dz = (Qj.ez - P.ez) + (Qj.lz - P.lz);
+            } else {
+                dx = Qj.ex - P.ex;
+                dy = Qj.ey - P.ey;
+                dz = Qj.ez - P.ez;
+            }
+            const VjpTerms<T> r = vjp_terms<T>(P, Qj, dx, dy, dz, eps2, diag && k == warp && st == 0);
+            vjp_acc_p<T>(y, r, Qj, dx, dy, dz);
+            vjp_acc_q<T>(z, r, P, dx, dy, dz);
+#pragma unroll
+            for (int c = 0; c < NY; ++c) z[c] = __shfl_sync(0xffffffffu, z[c], from);
+        }
+#pragma unroll
+        for (int c = 0; c < NY; ++c) qp[(warp * NY + c) * SYM_T + k * 32 + lane] = z[c];
+    }
+    __syncthreads();
+    const int q = q0 + tid;
+#pragma unroll
+    for (int c = 0; c < NY; ++c) {
+        const T zq = ((qp[c * SYM_T + tid] + qp[(NY + c) * SYM_T + tid]) + qp[(2 * NY + c) * SYM_T + tid]) +
+                     qp[(3 * NY + c) * SYM_T + tid];
+        if (diag) {
+            part[((size_t)I * NY + c) * a.npad + p] = T(0.5) * (y[c] + zq);
+        } else {
+            part[((size_t)J * NY + c) * a.npad + p] = y[c];   // row p, its pairs with tile J
+            part[((size_t)I * NY + c) * a.npad + q] = zq;     // row q, its pairs with tile I
+        }
+    }
+}
+
+// Per star: its sums over every tile (FP64, tile order) and the row outputs (split 0 of out).
+template <typename T>
+__global__ void __launch_bounds__(128) k_vjp_sym_rows(const PairVjpArgs a, const T *part, int nt) {
+    using V = typename VjpPack<T>::V;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nstar) return;
+    double Y[NY];
+    for (int c = 0; c < NY; ++c) Y[c] = 0.0;
+    for (int b = 0; b < nt; ++b)
+#pragma unroll
+        for (int c = 0; c < NY; ++c) Y[c] += (double)part[((size_t)b * NY + c) * a.npad + i];
+    VjpState<T> P;
+    vjp_load<T>(P, static_cast<const V *>(a.pack), static_cast<const V *>(a.apack), a.npad, i);
+    double o[NV_VJP];
+    vjp_row_out<T>(o, Y, P, 1.0 / sqrt(a.eps2));
+    for (int c = 0; c < NV_VJP; ++c) a.out[(size_t)c * a.npad + i] = o[c];
+}
+
 // ------------------------------------------------------------------ assembly
 struct AssembleArgs {
     const double *spos, *m, *vjp, *sdir, *vdir, *gbar;
@@ -562,7 +750,9 @@ struct AdjointWork {
     void *apack = nullptr;   // [6][npad] x 16 B
     double *sdir = nullptr, *vdir = nullptr, *vjp = nullptr, *gbar = nullptr, *part = nullptr;
     int vjp_splits = 0;
-    int g_best = 1, g_nstar = -1, g_f32 = -1;  // split count of the VJP sweep for this size
+    int g_best = 1, g_nstar = -1, g_f32 = -1;  // split count of the ordered VJP sweep for this size
+    void *sympart = nullptr;  // [tiles][NY][npad] partial sums of the symmetric sweep
+    size_t sym_bytes = 0;
     double *m0bar = nullptr;
     unsigned *tickets = nullptr;
     double *work = nullptr;  // [12][3][ld]: Xb Vb xb vb x1b v1b x2b v2b ab xF vF spare
@@ -581,7 +771,7 @@ void free_adjoint(pn_ctx *c) {
     AdjointWork *w = c->adj;
     if (!w) return;
     void *b[] = {w->sums, w->apack, w->sdir, w->vdir, w->vjp, w->gbar, w->part, w->m0bar, w->tickets,
-                 w->work, w->ckpt, w->seg, w->segsums};
+                 w->work, w->ckpt, w->seg, w->segsums, w->sympart};
     for (void *p : b)
         if (p) cudaFree(p);
     delete w;
@@ -619,7 +809,12 @@ static int adj_ensure(pn_ctx *c) {
     return PN_OK;
 }
 
-static int vjp_tj(const pn_ctx *c) { return is_f32(c) ? 128 : 64; }
+// Tile of the pack and of the ordered adjoint sweep.  The symmetric sweep's tiles are SYM_T
+// stars: in mixed precision they must be the pack's tiles (the FP32 positions are relative to
+// each tile's origin); the FP64 pack holds BH-relative positions and has no tile origins.
+static int vjp_tj(const pn_ctx *c) { return is_f32(c) ? SYM_T : 64; }
+// Largest per-tile partial-sum array of the symmetric sweep (larger systems take the ordered one).
+constexpr size_t kSymPartMax = (size_t)6 << 30;
 
 // VJP of one force evaluation at (x, v) (SoA, leading dim ld), whose pair sums are in `sums`
 // ([9][npad]).  abar: SoA [3][ld].  Writes (accumulate=0) or adds (1) xbar, vbar (SoA) and
@@ -652,35 +847,54 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
     const int nbf = (pa.nfill + VJP_ON_NT - 1) / VJP_ON_NT;
     k_finish_vjp<<<nbf, VJP_ON_NT, 0, s>>>(fa);
     CU(cudaGetLastError());
-    // O(N^2) sweep
+    // O(N^2) sweep: the symmetric form (each unordered pair once) unless its per-tile partial
+    // sums would take more than kSymPartMax bytes, or PN_VJP_SWEEP=ordered asks for the ordered one
     const int ntiles = nstar > 0 ? (nstar + tj - 1) / tj : 0;
-    const int nib = (nstar + VJP_NT - 1) / VJP_NT;
-    // j-range splits: the count whose CTAs fill the resident slots in the fewest tile-times,
-    // waves x tiles per CTA (a wave of small systems leaves SMs idle otherwise)
-    if (w->g_nstar != nstar || w->g_f32 != (int)f32) {
-        int dev = 0, sms = 0, per = 0;
-        CU(cudaGetDevice(&dev));
-        CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        const size_t smem = 128 + 2 * (size_t)(f32 ? VjpPack<float>::NGF + VjpPack<float>::NGA
-                                                    : VjpPack<double>::NGF + VjpPack<double>::NGA) * tj * 16;
-        CU(f32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pair_vjp<float>, VJP_NT, smem)
-               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pair_vjp<double>, VJP_NT, smem));
-        const long long slots = (long long)sms * (per > 0 ? per : 1);
-        int best = 1;
-        long long best_cost = -1;
-        for (int gc = 1; gc <= 64 && gc <= (ntiles > 0 ? ntiles : 1); ++gc) {
-            const long long waves = ((long long)nib * gc + slots - 1) / slots;
-            const long long cost = waves * ((ntiles + gc - 1) / gc);
-            if (best_cost < 0 || cost < best_cost) {
-                best_cost = cost;
-                best = gc;
+    const int nt_sym = nstar > 0 ? (nstar + SYM_T - 1) / SYM_T : 0;
+    const size_t tsize = f32 ? sizeof(float) : sizeof(double);
+    const size_t sym_bytes = (size_t)nt_sym * NY * c->npad * tsize;
+    const char *sweep_env = getenv("PN_VJP_SWEEP");
+    const bool ordered = sweep_env && !strcmp(sweep_env, "ordered");
+    const bool sym = nstar > 0 && !ordered && sym_bytes <= kSymPartMax && (!f32 || tj == SYM_T);
+    int g = 1;
+    if (sym) {
+        if (sym_bytes > w->sym_bytes) {
+            if (w->sympart) cudaFree(w->sympart);
+            w->sympart = nullptr;
+            w->sym_bytes = 0;
+            if (cudaMalloc(&w->sympart, sym_bytes) != cudaSuccess) {
+                cudaGetLastError();
+                return set_err(PN_ERR_NOMEM, "vjp tile partials: %zu bytes", sym_bytes);
             }
+            w->sym_bytes = sym_bytes;
         }
-        w->g_best = best;
-        w->g_nstar = nstar;
-        w->g_f32 = (int)f32;
+    } else {
+        const int nib = (nstar + VJP_NT - 1) / VJP_NT;
+        // j-range splits: the count whose CTAs fill the resident slots in the fewest tile-times,
+        // waves x tiles per CTA (a wave of small systems leaves SMs idle otherwise)
+        if (w->g_nstar != nstar || w->g_f32 != (int)f32) {
+            int per = 0;
+            const size_t smem = 128 + 2 * (size_t)(f32 ? VjpPack<float>::NGF + VjpPack<float>::NGA
+                                                        : VjpPack<double>::NGF + VjpPack<double>::NGA) * tj * 16;
+            CU(f32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pair_vjp<float>, VJP_NT, smem)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pair_vjp<double>, VJP_NT, smem));
+            const long long slots = (long long)c->sms * (per > 0 ? per : 1);
+            int best = 1;
+            long long best_cost = -1;
+            for (int gc = 1; gc <= 64 && gc <= (ntiles > 0 ? ntiles : 1); ++gc) {
+                const long long waves = ((long long)nib * gc + slots - 1) / slots;
+                const long long cost = waves * ((ntiles + gc - 1) / gc);
+                if (best_cost < 0 || cost < best_cost) {
+                    best_cost = cost;
+                    best = gc;
+                }
+            }
+            w->g_best = best;
+            w->g_nstar = nstar;
+            w->g_f32 = (int)f32;
+        }
+        g = w->g_best;
     }
-    const int g = w->g_best;
     if (g > w->vjp_splits) {
         if (w->vjp) cudaFree(w->vjp);
         w->vjp = nullptr;
@@ -696,25 +910,53 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
         qa.pack = c->pack; qa.apack = w->apack; qa.torg = c->torg; qa.spos = c->spos; qa.out = w->vjp;
         qa.err = c->err; qa.nstar = nstar; qa.npad = c->npad; qa.tj = tj; qa.ntiles = ntiles; qa.gsplit = g;
         qa.eps2 = eps2;
-        dim3 grid((unsigned)nib, (unsigned)g);
-        if (f32) {
-            const size_t smem = 128 + 2 * (size_t)(VjpPack<float>::NGF + VjpPack<float>::NGA) * tj * 16;
-            static size_t configured = 0;
-            if (smem > 48 * 1024 && smem > configured) {
-                CU(cudaFuncSetAttribute(k_pair_vjp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                configured = smem;
+        if (sym) {
+            const unsigned items = (unsigned)((long long)nt_sym * (nt_sym + 1) / 2);
+            const unsigned nbr = (unsigned)((nstar + 127) / 128);
+            if (f32) {
+                const size_t smem = sym_smem_bytes<float>();
+                static size_t configured = 0;
+                if (smem > 48 * 1024 && smem > configured) {
+                    CU(cudaFuncSetAttribute(k_pair_vjp_sym<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                    configured = smem;
+                }
+                k_pair_vjp_sym<float><<<items, SYM_T, smem, s>>>(qa, static_cast<float *>(w->sympart));
+                CU(cudaGetLastError());
+                k_vjp_sym_rows<float><<<nbr, 128, 0, s>>>(qa, static_cast<const float *>(w->sympart), nt_sym);
+            } else {
+                const size_t smem = sym_smem_bytes<double>();
+                static size_t configured = 0;
+                if (smem > 48 * 1024 && smem > configured) {
+                    CU(cudaFuncSetAttribute(k_pair_vjp_sym<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                    configured = smem;
+                }
+                k_pair_vjp_sym<double><<<items, SYM_T, smem, s>>>(qa, static_cast<double *>(w->sympart));
+                CU(cudaGetLastError());
+                k_vjp_sym_rows<double><<<nbr, 128, 0, s>>>(qa, static_cast<const double *>(w->sympart), nt_sym);
             }
-            k_pair_vjp<float><<<grid, VJP_NT, smem, s>>>(qa);
+            CU(cudaGetLastError());
         } else {
-            const size_t smem = 128 + 2 * (size_t)(VjpPack<double>::NGF + VjpPack<double>::NGA) * tj * 16;
-            static size_t configured = 0;
-            if (smem > 48 * 1024 && smem > configured) {
-                CU(cudaFuncSetAttribute(k_pair_vjp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                configured = smem;
+            const int nib = (nstar + VJP_NT - 1) / VJP_NT;
+            dim3 grid((unsigned)nib, (unsigned)g);
+            if (f32) {
+                const size_t smem = 128 + 2 * (size_t)(VjpPack<float>::NGF + VjpPack<float>::NGA) * tj * 16;
+                static size_t configured = 0;
+                if (smem > 48 * 1024 && smem > configured) {
+                    CU(cudaFuncSetAttribute(k_pair_vjp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                    configured = smem;
+                }
+                k_pair_vjp<float><<<grid, VJP_NT, smem, s>>>(qa);
+            } else {
+                const size_t smem = 128 + 2 * (size_t)(VjpPack<double>::NGF + VjpPack<double>::NGA) * tj * 16;
+                static size_t configured = 0;
+                if (smem > 48 * 1024 && smem > configured) {
+                    CU(cudaFuncSetAttribute(k_pair_vjp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                    configured = smem;
+                }
+                k_pair_vjp<double><<<grid, VJP_NT, smem, s>>>(qa);
             }
-            k_pair_vjp<double><<<grid, VJP_NT, smem, s>>>(qa);
+            CU(cudaGetLastError());
         }
-        CU(cudaGetLastError());
     }
     AssembleArgs aa{};
     aa.spos = c->spos; aa.m = c->st.m; aa.vjp = w->vjp; aa.sdir = w->sdir; aa.vdir = w->vdir; aa.gbar = w->gbar;

@@ -914,7 +914,7 @@ extern "C" int pn_bench_steps(pn_ctx *c, int nsteps, int flush_l2, double *step_
 extern "C" double pn_flops_per_pair(int mode, int precision, int pair_variant) {
     const bool f32 = precision == PN_PREC_MIXED;
     if (f32 && pair_variant == PN_PAIR_F32X2) {
-        // the packed sweep (operands pre-scaled): FORCE 51 FP32 operations of which 23 FMA,
+        // the packed sweep (operands pre-scaled): FORCE 50 FP32 operations of which 24 FMA,
         // NEWTON 22 (7 FMA), ENERGY 32 (12 FMA); FMA = 2 flops, the MUFU rsqrt = 1
         switch (mode) {
             case MODE_NEWTON: return 30.0;

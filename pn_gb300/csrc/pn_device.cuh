@@ -75,10 +75,21 @@ enum AccSlotE : int { E_PHI = 0, E_PSI = 1 };
 constexpr double X2_K = 2965821.0 / 4194304.0;
 constexpr double X2_SQRT3 = 1.7320508075688772935;
 
-// FP64 origin of one j-tile (BH-relative), 32-byte aligned for one vector load.
+// Origin of one j-tile (BH-relative): FP64, and the same split into an FP32 pair
+// (h = fl32(x), l = fl32(x - h)) for sweeps that form (s_i - o) without FP64 arithmetic.
 struct __align__(32) TileOrigin {
     double x, y, z, w;
+    float hx, hy, hz, lx, ly, lz, pad0, pad1;
 };
+
+// Exact FP32 difference a - b as s + err (Knuth's TwoSum; no multiplications, so nothing is
+// contracted into an FMA).
+__device__ __forceinline__ float two_diff(float a, float b, float &err) {
+    const float s = a - b;
+    const float bb = s - a;
+    err = (a - (s - bb)) - (b + bb);
+    return s;
+}
 
 // ------------------------------------------------------------------ device error word bits
 enum DevErr : int { DEVERR_TIMEOUT = 1, DEVERR_NONFINITE = 2 };

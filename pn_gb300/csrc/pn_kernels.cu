@@ -171,7 +171,14 @@ __device__ __forceinline__ void prep_body(const PrepArgs &a, int blk, int nblk) 
                 }
                 a.ipack[j] = make_float4((float)vv[0], (float)vv[1], (float)vv[2], (float)qe);
             }
-            if (j % a.tj == 0 && real) a.torg[j / a.tj] = TileOrigin{s[0], s[1], s[2], 0.0};
+            if (j % a.tj == 0 && real) {
+                TileOrigin o{s[0], s[1], s[2], 0.0};
+                o.hx = (float)s[0]; o.lx = (float)(s[0] - (double)o.hx);
+                o.hy = (float)s[1]; o.ly = (float)(s[1] - (double)o.hy);
+                o.hz = (float)s[2]; o.lz = (float)(s[2] - (double)o.hz);
+                o.pad0 = o.pad1 = 0.f;
+                a.torg[j / a.tj] = o;
+            }
         } else {
             double2 *pk = static_cast<double2 *>(a.pack);
             pk[j] = make_double2(s[0], s[1]);

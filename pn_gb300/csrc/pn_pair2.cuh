@@ -14,7 +14,7 @@
 // (primed = odd star), so one 128-bit shared load yields two f32x2 operands.  The entries are
 // scaled (pn_device.cuh, X2_K): mK = m / K^3, mu3K = mu3 / K, k35K = k35 / K, w = sqrt(3) v,
 // c1v = c1 - 2 |v|^2.  With the sweep's Q' = K Q these fold every constant factor of the pair
-// expressions into data: 51 FP32 operations per force pair instead of 56, and
+// expressions into data: 50 FP32 operations per force pair instead of 56, and
 //   br = (rhoe - qe) c3 + c1 + |v_i|^2 - 2 |dv|^2 + 1.5 vdj^2 Q^2
 //      = (rhoe - qe) c3 + c1v + (vi* . w_j - |v_i|^2) + (w_j . d)^2 Q'^2      (vi* = 4 v_i / sqrt(3))
 //   sum_j cv dv = sum_j ct w_j - 0.75 vi* sum_j ct,  ct = mQ^3 (vi* . d - w_j . d) = cv / sqrt(3)
@@ -111,7 +111,7 @@ __device__ __forceinline__ void pair2_accumulate(f2 *acc, const I2 &I, f2 jx, f2
         acc[A_GZ] = fma2(mQ3, dz, acc[A_GZ]);
         acc[A_PHI] = add2(acc[A_PHI], mQ);
         acc[A_S0] = add2(acc[A_S0], mQ3);
-        acc[A_U] = add2(acc[A_U], mul2(jmu3, Q));
+        acc[A_U] = fma2(jmu3, Q, acc[A_U]);
         const f2 vivj = fma2(I.vz, jwz, fma2(I.vy, jwy, fma2(I.vx, jwx, I.nvi2)));  // 4 vi.vj - vi^2
         const f2 vdj = fma2(jwz, dz, fma2(jwy, dy, mul2(jwx, dx)));                // sqrt(3) vj.d
         const f2 vdi = fma2(I.vz, dz, fma2(I.vy, dy, mul2(I.vx, dx)));             // 4/sqrt(3) vi.d
@@ -146,6 +146,19 @@ template <int MODE> struct Mode2 {
     static constexpr int PHI = mode_has_force(MODE) ? (int)A_PHI : (MODE == MODE_ENERGY ? (int)E_PHI : -1);
 };
 
+// Kahan running sums of the per-i tile partials, kept in shared memory (they are touched once
+// per tile), [2 (sum, compensation)][NACC][IPT][PAIR_NT] floats after the two mbarriers; the
+// tile buffers follow at a fixed offset, so the ensemble kernel's per-cluster tile sizes need no
+// runtime layout.
+template <int MODE, int IPT>
+__host__ __device__ constexpr size_t pair2_kahan_bytes() {
+    return (size_t)2 * ModeInfo<MODE>::NACC * IPT * PAIR_NT * sizeof(float);
+}
+template <int MODE, int IPT>
+inline size_t pair2_smem_bytes(int tj) {
+    return 128 + pair2_kahan_bytes<MODE, IPT>() + 2 * (size_t)Mode2<MODE>::NG * (size_t)(tj / 2) * 16;
+}
+
 // Resident CTAs per SM the register budget is sized for: 4 at IPT = 1 (<= 128 registers); at
 // IPT = 2 either 2 (no register cap, ~196) or 3 (<= 168 registers), both offered to the tuner
 // (PairCfg::x2 = 1 or 2).
@@ -160,7 +173,7 @@ constexpr int pair2_min_blocks() {
 // i-side float4 (v.xyz, qe) array.
 template <int MODE, int IPT>
 __device__ __forceinline__ bool pair2_block(const PairArgs &a, int ibase, int split, uint64_t *bars,
-                                            float4 *buf, uint32_t &seq) {
+                                            float *kahan, float4 *buf, uint32_t &seq) {
     constexpr int NT = PAIR_NT;
     constexpr int NG = Mode2<MODE>::NG;
     constexpr int NACC = ModeInfo<MODE>::NACC;
@@ -174,14 +187,20 @@ __device__ __forceinline__ bool pair2_block(const PairArgs &a, int ibase, int sp
     const f2 eps2 = f2_bcast((float)a.eps2);
 
     I2 I[IPT];
-    double sx[IPT], sy[IPT], sz[IPT];
+    // the i position (BH-relative) as an FP32 pair, split once; per tile, s_i - o_t is formed
+    // from it and the tile origin's FP32 pair by an exact difference (two_diff), with no FP64
+    // arithmetic in the tile loop
+    float shx[IPT], shy[IPT], shz[IPT], slx[IPT], sly[IPT], slz[IPT];
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
         const int i = ibase + tid + k * NT;
         const bool valid = i < a.nstar;
-        sx[k] = valid ? a.spos[i] : 0.0;
-        sy[k] = valid ? a.spos[a.npad + i] : 0.0;
-        sz[k] = valid ? a.spos[2 * a.npad + i] : 0.0;
+        const double sx = valid ? a.spos[i] : 0.0;
+        const double sy = valid ? a.spos[a.npad + i] : 0.0;
+        const double sz = valid ? a.spos[2 * a.npad + i] : 0.0;
+        shx[k] = (float)sx; slx[k] = (float)(sx - (double)shx[k]);
+        shy[k] = (float)sy; sly[k] = (float)(sy - (double)shy[k]);
+        shz[k] = (float)sz; slz[k] = (float)(sz - (double)shz[k]);
         float vx = 0.f, vy = 0.f, vz = 0.f, qe = 0.f;
         if (MODE != MODE_NEWTON && valid) {
             const float4 g = a.ipack[i];
@@ -194,11 +213,14 @@ __device__ __forceinline__ bool pair2_block(const PairArgs &a, int ibase, int sp
         I[k].qe = f2_bcast(qe);
         I[k].nvi2 = f2_bcast(-fmaf(vz, vz, fmaf(vy, vy, vx * vx)));
     }
-    float run[IPT][NACC], cmp[IPT][NACC];
+    // Kahan state of (slot q, i k) of this thread at kahan[q][k][tid] (sum) and
+    // kahan[NACC + q][k][tid] (compensation)
+    auto ksum = [&](int q, int k) -> float & { return kahan[(q * IPT + k) * NT + tid]; };
+    auto kcmp = [&](int q, int k) -> float & { return kahan[((NACC + q) * IPT + k) * NT + tid]; };
 #pragma unroll
     for (int k = 0; k < IPT; ++k)
 #pragma unroll
-        for (int q = 0; q < NACC; ++q) run[k][q] = cmp[k][q] = 0.f;
+        for (int q = 0; q < NACC; ++q) ksum(q, k) = kcmp(q, k) = 0.f;
 
     const uint32_t gbytes = (uint32_t)tp * 16u;
     auto issue = [&](int t, int stage) {
@@ -226,17 +248,22 @@ __device__ __forceinline__ bool pair2_block(const PairArgs &a, int ibase, int sp
             return false;
         }
         {
-            const TileOrigin o = a.torg[t];
+            // s_i - o_t = (sh - oh) + (sl - ol): the hi difference exactly (two_diff), its error
+            // and the lo difference in the lo part
+            const TileOrigin &o = a.torg[t];
+            const float ohx = o.hx, ohy = o.hy, ohz = o.hz, olx = o.lx, oly = o.ly, olz = o.lz;
 #pragma unroll
             for (int k = 0; k < IPT; ++k) {
-                const double rx = sx[k] - o.x, ry = sy[k] - o.y, rz = sz[k] - o.z;
-                const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
+                float ex, ey, ez;
+                const float hx = two_diff(shx[k], ohx, ex);
+                const float hy = two_diff(shy[k], ohy, ey);
+                const float hz = two_diff(shz[k], ohz, ez);
                 I[k].ex = f2_bcast(hx);
                 I[k].ey = f2_bcast(hy);
                 I[k].ez = f2_bcast(hz);
-                I[k].lx = f2_bcast((float)(rx - (double)hx));
-                I[k].ly = f2_bcast((float)(ry - (double)hy));
-                I[k].lz = f2_bcast((float)(rz - (double)hz));
+                I[k].lx = f2_bcast(ex + (slx[k] - olx));
+                I[k].ly = f2_bcast(ey + (sly[k] - oly));
+                I[k].lz = f2_bcast(ez + (slz[k] - olz));
             }
         }
         const float4 *b = buf + (size_t)stage * NG * tp;
@@ -279,7 +306,12 @@ __device__ __forceinline__ bool pair2_block(const PairArgs &a, int ibase, int sp
                 ts[A_WZ] = fmaf(c, wz, ts[A_WZ]);
             }
 #pragma unroll
-            for (int q = 0; q < NACC; ++q) kahan_add(run[k][q], cmp[k][q], ts[q]);
+            for (int q = 0; q < NACC; ++q) {
+                float sum = ksum(q, k), comp = kcmp(q, k);
+                kahan_add(sum, comp, ts[q]);
+                ksum(q, k) = sum;
+                kcmp(q, k) = comp;
+            }
         }
         __syncthreads();
     }
@@ -290,7 +322,7 @@ __device__ __forceinline__ bool pair2_block(const PairArgs &a, int ibase, int sp
             double val[NACC];
 #pragma unroll
             for (int q = 0; q < NACC; ++q)
-                val[q] = ((double)run[k][q] - (double)cmp[k][q]) * (q == Mode2<MODE>::PHI ? X2_K * X2_K : 1.0);
+                val[q] = ((double)ksum(q, k) - (double)kcmp(q, k)) * (q == Mode2<MODE>::PHI ? X2_K * X2_K : 1.0);
             if constexpr (MODE == MODE_FORCE_ENERGY) {
                 float nvi2, u;
                 f2_unpack(I[k].nvi2, nvi2, u);
@@ -308,7 +340,8 @@ template <int MODE, int IPT, int OCC>
 __global__ void __launch_bounds__(PAIR_NT, (pair2_min_blocks<IPT, OCC>())) k_pair2(const PairArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
-    float4 *buf = reinterpret_cast<float4 *>(smem + 128);
+    float *kahan = reinterpret_cast<float *>(smem + 128);
+    float4 *buf = reinterpret_cast<float4 *>(smem + 128 + pair2_kahan_bytes<MODE, IPT>());
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
@@ -316,7 +349,7 @@ __global__ void __launch_bounds__(PAIR_NT, (pair2_min_blocks<IPT, OCC>())) k_pai
     }
     __syncthreads();
     uint32_t seq = 0;
-    pair2_block<MODE, IPT>(a, blockIdx.x * (PAIR_NT * IPT), blockIdx.y, bars, buf, seq);
+    pair2_block<MODE, IPT>(a, blockIdx.x * (PAIR_NT * IPT), blockIdx.y, bars, kahan, buf, seq);
 }
 
 // Ensemble form: one persistent launch over the work items of every cluster, as k_pair_ens
@@ -327,7 +360,8 @@ __global__ void __launch_bounds__(PAIR_NT, (pair2_min_blocks<IPT, 2>()))
     k_pair2_ens(const PairArgs *tab, const int4 *items, int nitems, unsigned *counter) {
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
-    float4 *buf = reinterpret_cast<float4 *>(smem + 128);
+    float *kahan = reinterpret_cast<float *>(smem + 128);
+    float4 *buf = reinterpret_cast<float4 *>(smem + 128 + pair2_kahan_bytes<MODE, IPT>());
     __shared__ int cur;
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], 1);
@@ -345,7 +379,7 @@ __global__ void __launch_bounds__(PAIR_NT, (pair2_min_blocks<IPT, 2>()))
         const int4 it = items[w];
         PairArgs a = tab[it.x];
         a.pack = a.pack2;
-        if (!pair2_block<MODE, IPT>(a, it.y, it.z, bars, buf, seq)) break;
+        if (!pair2_block<MODE, IPT>(a, it.y, it.z, bars, kahan, buf, seq)) break;
     }
 }
 

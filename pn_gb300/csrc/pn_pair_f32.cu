@@ -9,7 +9,7 @@ template <int MODE, int IPT, int OCC>
 static cudaError_t launch_two(const PairCfg &c, const PairArgs &a0, cudaStream_t s) {
     PairArgs a = a0;
     a.pack = a0.pack2;
-    const size_t smem = 128 + 2 * (size_t)Mode2<MODE>::NG * (size_t)(c.tj / 2) * 16;
+    const size_t smem = pair2_smem_bytes<MODE, IPT>(c.tj);
     auto fn = k_pair2<MODE, IPT, OCC>;
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
@@ -134,7 +134,7 @@ static cudaError_t launch_ens_mode(int ipt, int js, int tjmax, int grid, const P
 template <int MODE, int IPT>
 static cudaError_t launch_ens_two(int tjmax, int grid, const PairArgs *tab, const int4 *items, int nitems,
                                   unsigned *counter, cudaStream_t s) {
-    const size_t smem = 128 + 2 * (size_t)Mode2<MODE>::NG * (size_t)(tjmax / 2) * 16;
+    const size_t smem = pair2_smem_bytes<MODE, IPT>(tjmax);
     auto fn = k_pair2_ens<MODE, IPT>;
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {

@@ -148,3 +148,28 @@ def test_trajectory_gradient_fd(pn, K):
     mm[0] -= h
     fd = (run_loss(pn, x, v, mp, eps, dt, nsteps, xt, vt) - run_loss(pn, x, v, mm, eps, dt, nsteps, xt, vt)) / (2 * h)
     assert abs(gm - fd) <= 1e-6 * max(abs(fd), 1e-3), (gm, fd)
+
+
+@pytest.mark.parametrize("n", [2, 129, 300, 1025])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_symmetric_sweep_equals_ordered_sweep(pn, monkeypatch, n, prec):
+    """The symmetric VJP sweep (each unordered pair once, one CTA per pair of 128-star tiles, the
+    row sums of q carried lane to lane) against the ordered sweep (each row over every star),
+    selected with PN_VJP_SWEEP: the same sums in another order, at ragged sizes (one tile, a
+    partial last tile, several tiles), FP64 and mixed, at c = 1 and with the weak 1PN terms."""
+    x, v, m = system(n, 40 + n)
+    abar = np.random.default_rng(n).normal(size=x.shape)
+    for ic2 in (1.0, 1e-6):
+        out = {}
+        for mode in ("ordered", "symmetric"):
+            monkeypatch.setenv("PN_VJP_SWEEP", mode)
+            with pn.Context(n, eps=0.02, precision=prec, inv_c2=ic2) as c:
+                c.set_state(x, v, m)
+                out[mode] = c.force_vjp(abar)
+        tol = 1e-12 if prec == 0 else 1e-5
+        for k in (0, 1):
+            a, b = out["symmetric"][k], out["ordered"][k]
+            d = np.linalg.norm(a - b, axis=1)
+            ref = np.linalg.norm(b, axis=1)
+            assert np.sqrt((d ** 2).mean() / max((ref ** 2).mean(), 1e-300)) <= tol, (ic2, k)
+        assert abs(out["symmetric"][2] - out["ordered"][2]) <= tol * abs(out["ordered"][2]) + 1e-300, ic2

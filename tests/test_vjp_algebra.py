@@ -154,3 +154,69 @@ def test_factored_row_sums_equal_plain_sums():
     for p in (0, 7, 41):
         a, b = plain_row(p), factored_row(p)
         assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max(), (p, np.abs(a - b).argmax())
+
+
+def _row_out(p, Y):
+    """The per-row finish of the factored sums (vjp_row_out), self pair's mu3 term included."""
+    Sacc, Vacc = Y[0:3], Y[3:6]
+    A, B, Sg, Scv, QE, S0s, Sg2, Sb2, MU3, C3, K35 = Y[6:]
+    sb = Sacc - G[p] * S0s - 4 * v[p] * A - W[p] * B + v[p] * Sb2
+    vb = Vacc - 2 * v[p] * Sg - W[p] * Scv - 4 * v[p] * Sg2
+    return np.concatenate([sb, vb, [-QE, MU3 + U[p] / np.sqrt(EPS2), Sg2, C3, K35]])
+
+
+def symmetric_rows():
+    """The symmetric sweep's form: each unordered pair {p, q} visited once; the intermediates of
+    the two pair terms F(p, q) and F(q, p) serve row p (y) and row q (z, the same sums with
+    d -> -d and the two terms' roles exchanged)."""
+    Y = np.zeros((N, 17))
+    vi2 = (v * v).sum(1)
+    cW = (W * v).sum(1)
+    for p in range(N):
+        for q in range(p + 1, N):
+            d = s[q] - s[p]
+            rho = d @ d + EPS2
+            Q = rho ** -0.5
+            Q2, Q3 = Q * Q, Q ** 3
+            vdp, vdq, vpq = v[p] @ d, v[q] @ d, v[p] @ v[q]
+            dv2 = vi2[p] + vi2[q] - 2 * vpq
+            rp = rho - qe[p]
+            mQ3 = m[q] * Q3
+            gd, wd, wdv = G[p] @ d, W[p] @ d, W[p] @ v[q] - cW[p]
+            br = c1[q] + c3[q] * rp + vi2[p] - 2 * dv2 + 1.5 * vdq ** 2 * Q2
+            k4 = 4 * vdp - 3 * vdq
+            cd, cv = mQ3 * br + k35[q] * Q, mQ3 * k4
+            LQ = (3 * m[q] * Q2 * (gd + S0[p] + br * wd + k4 * wdv) + Phi[p] * m[q] + U[p] * mu3[q]
+                  + wd * (3 * mQ3 * vdq ** 2 * Q + k35[q]))
+            ga, h = mQ3 * wd, mQ3 * wdv
+            al = 2 * c3[q] * ga - LQ * Q3
+            be = 3 * (Q2 * vdq * ga - h)
+            mQ3b = m[p] * Q3
+            gq, wq = G[q] @ d, W[q] @ d
+            wdv2 = W[q] @ v[p] - cW[q]
+            rq = rho - qe[q]
+            br2 = c1[p] + c3[p] * rq + vi2[q] - 2 * dv2 + 1.5 * vdp ** 2 * Q2
+            k42 = 3 * vdp - 4 * vdq
+            cd2, cv2 = mQ3b * br2 + k35[p] * Q, mQ3b * k42
+            LQ2 = (3 * m[p] * Q2 * (-gq + S0[q] - br2 * wq + k42 * wdv2) + Phi[q] * m[p] + U[q] * mu3[p]
+                   - wq * (3 * mQ3b * vdp ** 2 * Q + k35[p]))
+            ga2, h2 = -mQ3b * wq, mQ3b * wdv2
+            al2 = 2 * c3[p] * ga2 - LQ2 * Q3
+            be2 = -3 * (Q2 * vdp * ga2 + h2)
+            cS, cSv, cV, cVd = -(al + al2), 4 * h2 - be, 4 * (ga + ga2), 4 * h - be2
+            y = Y[p]
+            y[0:3] += cS * d + cSv * v[q] + mQ3b * G[q] + cd2 * W[q]
+            y[3:6] += cV * v[q] + cVd * d + cv2 * W[q]
+            y[6:] += [h, cd, ga, cv, c3[q] * ga, mQ3, ga2, be2, U[q] * Q, ga2 * rq, -Q * wq]
+            z = Y[q]
+            z[0:3] += -cS * d + cVd * v[p] + mQ3 * G[p] + cd * W[p]
+            z[3:6] += cV * v[p] - cSv * d + cv * W[p]
+            z[6:] += [h2, cd2, ga2, cv2, c3[p] * ga2, mQ3b, ga, be, U[p] * Q, ga * rp, Q * wd]
+    return np.array([_row_out(p, Y[p]) for p in range(N)])
+
+
+def test_symmetric_sweep_equals_plain_sums():
+    rows = symmetric_rows()
+    for p in (0, 7, 41, N - 1):
+        a = plain_row(p)
+        assert np.abs(rows[p] - a).max() <= 1e-12 * np.abs(a).max(), (p, np.abs(rows[p] - a).argmax())
