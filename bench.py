@@ -505,13 +505,14 @@ def long_run(nstars, precisions, nsteps, every, allowance, label):
 
 def profile_case(nstars, shape=None):
     """One mixed-precision force evaluation of the bench workload at nstars (ncu target);
-    shape = "ipt,tile_j,grid_split" pins the packed sweep's launch shape (e.g. the tuned one)."""
+    shape = "ipt,tile_j,grid_split[,pair_variant]" pins the packed sweep's launch shape (e.g. the
+    tuned one; pair_variant 3 = the build for 3 CTAs per SM)."""
     import pn_gb300 as pn
     sysm = pn.config_plummer(nstars, SEED, BH_FRACTION)
     kw = {}
     if shape:
-        ipt, tj, gs = (int(t) for t in shape.split(","))
-        kw = dict(i_per_thread=ipt, tile_j=tj, grid_split=gs, pair_variant=2)
+        f = [int(t) for t in shape.split(",")]
+        kw = dict(i_per_thread=f[0], tile_j=f[1], grid_split=f[2], pair_variant=f[3] if len(f) > 3 else 2)
     with pn.Context(nstars + 1, eps=plummer_eps(nstars), inv_c2=INV_C2,
                     precision=pn.PN_PREC_MIXED, **kw) as c:
         c.set_state(sysm.x, sysm.v, sysm.m)
@@ -587,7 +588,8 @@ def headline(args, rank, world, dist):
         peak32 = pn.probe_fma_peak(pn.PN_PREC_MIXED)
         pairs = float(ns) * float(ns)
         achieved = pairs * flops_pair / (pair_launch_ms * 1e-3) / 1e12
-        kname = "k_pair2<MODE_FORCE> (packed f32x2)" if st.pair_variant == 2 else "k_pair<float, MODE_FORCE>"
+        kname = {2: "k_pair2<MODE_FORCE> (packed f32x2)",
+                 3: "k_pair2<MODE_FORCE> (packed f32x2, 3 CTAs per SM)"}.get(st.pair_variant, "k_pair<float, MODE_FORCE>")
         line["roofline"] = {"bound": "fp32", "kernel": kname,
                             "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                             "frac": achieved / peak32, "traffic": None,
@@ -596,7 +598,7 @@ def headline(args, rank, world, dist):
                             "peak_source": "measured FP32 FMA throughput of this GPU (pn_probe_fma_peak)",
                             "pair_interactions_per_s": pairs / (pair_launch_ms * 1e-3)}
         prof = os.path.join(ROOT, "profiles", "pair_sweep_traffic.json")
-        if os.path.exists(prof) and ns == NSTARS and st.pair_variant == 2:
+        if os.path.exists(prof) and ns == NSTARS and st.pair_variant in (2, 3):
             try:  # DRAM bytes of one launch at this size and shape, from an ncu capture
                 pt = json.load(open(prof))
                 line["roofline"]["traffic"] = pt.get("k_pair2_force_f32_N262144_bytes_per_launch")
@@ -717,7 +719,8 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--fd-coords", type=int, default=64)
     ap.add_argument("--fd-steps", type=int, default=40)
-    ap.add_argument("--shape", default=None, help="--profile-case launch shape: ipt,tile_j,grid_split")
+    ap.add_argument("--shape", default=None,
+                    help="--profile-case launch shape: ipt,tile_j,grid_split[,pair_variant]")
     ap.add_argument("--fp64-run", type=int, default=0, metavar="STEPS",
                     help="configuration 2 alone: N=65536, FP64 and mixed, STEPS steps each")
     ap.add_argument("--drift", type=int, default=0, metavar="STEPS",

@@ -115,10 +115,10 @@ static PairCfg choose_cfg(const pn_ctx *c, int mode, int nstar) {
         if (tuned.gsplit > ntiles_t) tuned.gsplit = ntiles_t;
         return tuned;
     }
-    if (pv == PN_PAIR_F32X2 && f32) {
+    if ((pv == PN_PAIR_F32X2 || pv == PN_PAIR_F32X2_OCC3) && f32) {
         if (k.ipt > 2) k.ipt = 2;
         if (k.js != 1) k.js = 1;
-        k.x2 = 1;
+        k.x2 = (pv == PN_PAIR_F32X2_OCC3 && k.ipt == 2 && mode_has_force(mode)) ? 2 : 1;
     } else if (pv == PN_PAIR_AUTO && f32 && !explicit_shape) {
         // untuned default of the mixed sweep: the packed f32x2 form, 2 i per thread for
         // N >= 4096 (fastest in the tuner's measurements at N = 2^18: 111 ms vs 125 ms)
@@ -198,7 +198,7 @@ static int validate_params(const pn_params *p) {
         return PN_ERR_INVALID;
     if (p->i_per_thread < 0 || p->j_split < 0 || p->grid_split < 0 || p->grid_split > 64)
         return PN_ERR_INVALID;
-    if (p->pair_variant < PN_PAIR_AUTO || p->pair_variant > PN_PAIR_F32X2) return PN_ERR_INVALID;
+    if (p->pair_variant < PN_PAIR_AUTO || p->pair_variant > PN_PAIR_F32X2_OCC3) return PN_ERR_INVALID;
     if (p->integrator != PN_INT_REFERENCE && p->integrator != PN_INT_RK4) return PN_ERR_INVALID;
     if ((p->i_per_thread || p->j_split) &&
         !pair_shape_supported(p->i_per_thread ? p->i_per_thread : 1, p->j_split ? p->j_split : 1))
@@ -359,7 +359,7 @@ int pn::eval_force(pn_ctx *c, const double *x, const double *v, const double *m,
     if (timed) CU(cudaEventRecord(c->ev2, s));
     c->stats.tile_j = k.tj; c->stats.i_per_thread = k.ipt; c->stats.j_split = k.js;
     c->stats.grid_split = k.gsplit; c->stats.threads = PAIR_NT;
-    c->stats.pair_variant = k.x2 ? PN_PAIR_F32X2 : PN_PAIR_SCALAR;
+    c->stats.pair_variant = k.x2 == 2 ? PN_PAIR_F32X2_OCC3 : k.x2 ? PN_PAIR_F32X2 : PN_PAIR_SCALAR;
     c->stats.interactions = (double)nstar * (double)nstar;
     return PN_OK;
 }
@@ -913,7 +913,7 @@ extern "C" int pn_bench_steps(pn_ctx *c, int nsteps, int flush_l2, double *step_
 // rsqrt as 1 and every other add/multiply as 1 (the operations written in pn_device.cuh).
 extern "C" double pn_flops_per_pair(int mode, int precision, int pair_variant) {
     const bool f32 = precision == PN_PREC_MIXED;
-    if (f32 && pair_variant == PN_PAIR_F32X2) {
+    if (f32 && (pair_variant == PN_PAIR_F32X2 || pair_variant == PN_PAIR_F32X2_OCC3)) {
         // the packed sweep (operands pre-scaled): FORCE 50 FP32 operations of which 24 FMA,
         // NEWTON 22 (7 FMA), ENERGY 32 (12 FMA); FMA = 2 flops, the MUFU rsqrt = 1
         switch (mode) {
@@ -1026,16 +1026,35 @@ extern "C" int pn_autotune(pn_ctx *c, int sweeps, double *best_ms) {
             qa.nstar = nstar; qa.npad = c->npad; qa.tj = k.tj; qa.ntiles = (nstar + k.tj - 1) / k.tj;
             qa.gsplit = k.gsplit; qa.eps2 = eps2;
             float t = 1e30f;
-            for (int rep = 0; rep < 2; ++rep) {  // first launch warms up
-                CU(cudaEventRecord(c->ev0, c->stream));
-                cudaError_t e = f32 ? launch_pair_f32(mode, k, qa, c->stream)
-                                    : launch_pair_f64(mode, k, qa, c->stream);
-                if (e != cudaSuccess) return set_err(PN_ERR_CUDA, "autotune: %s", cudaGetErrorString(e));
-                CU(cudaEventRecord(c->ev1, c->stream));
-                CU(cudaEventSynchronize(c->ev1));
-                float ms = 0.f;
-                CU(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-                if (rep > 0) t = ms;
+            if (which == 0) {
+                // the force sweep: time the whole evaluation (prep, pair sweep, finish), so that
+                // the finishing kernel's reads of the j-range partial sums (72 B per star and
+                // split) count against the shapes with many splits
+                c->cfg_force = k;
+                c->cfg_energy = k;
+                c->cfg_set = true;
+                for (int rep = 0; rep < 3; ++rep) {  // first evaluation warms up; best of two
+                    CU(cudaEventRecord(c->ev0, c->stream));
+                    rc = eval_force(c, c->st.x, c->st.v, c->st.m, 1, c->ld, nullptr, 3, 1, 0, c->stream, false);
+                    if (rc) return rc;
+                    CU(cudaEventRecord(c->ev1, c->stream));
+                    CU(cudaEventSynchronize(c->ev1));
+                    float ms = 0.f;
+                    CU(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+                    if (rep > 0 && ms < t) t = ms;
+                }
+            } else {
+                for (int rep = 0; rep < 2; ++rep) {  // first launch warms up
+                    CU(cudaEventRecord(c->ev0, c->stream));
+                    cudaError_t e = f32 ? launch_pair_f32(mode, k, qa, c->stream)
+                                        : launch_pair_f64(mode, k, qa, c->stream);
+                    if (e != cudaSuccess) return set_err(PN_ERR_CUDA, "autotune: %s", cudaGetErrorString(e));
+                    CU(cudaEventRecord(c->ev1, c->stream));
+                    CU(cudaEventSynchronize(c->ev1));
+                    float ms = 0.f;
+                    CU(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+                    if (rep > 0) t = ms;
+                }
             }
             if (getenv("PN_TUNE_VERBOSE"))
                 fprintf(stderr, "pn_autotune mode %d: ipt %d js %d tj %d gsplit %d x2 %d: %.3f ms\n", mode,

@@ -216,8 +216,7 @@ __device__ __forceinline__ void pair_accumulate(T *acc, const IState<T> &I, T jx
         acc[A_GZ] = pn_fma(mQ3, dz, acc[A_GZ]);
         acc[A_PHI] += mQ;
         acc[A_S0] += mQ3;
-        const T uQ = jmu3 * Q;
-        acc[A_U] += uQ;
+        acc[A_U] = pn_fma(jmu3, Q, acc[A_U]);
         const T dvx = jvx - I.vx, dvy = jvy - I.vy, dvz = jvz - I.vz;
         const T dv2 = pn_fma(dvz, dvz, pn_fma(dvy, dvy, dvx * dvx));
         const T vdj = pn_fma(jvz, dz, pn_fma(jvy, dy, jvx * dx));

@@ -1,8 +1,10 @@
 // pn_tune.cu -- launch-shape autotuner of the pair sweep.
 //
 // A shape is (i per thread, lanes per i-set, j-tile size, j-range splits).  The tuner times a
-// candidate list on real data (CUDA events around the pair launch only, one warm-up launch per
-// shape) and keeps the fastest per key (precision, sweep mode, size class = floor(log2 N)).
+// candidate list on real data (CUDA events; the force sweep as a whole evaluation, so that the
+// cost of reading back many j-range partial sums counts, the energy sweep as its pair launch;
+// one warm-up per shape) and keeps the fastest per key (precision, sweep mode, size class =
+// floor(log2 N)).
 // Results live in a process-wide table; with PN_TUNE_CACHE=<file> they are also read from and
 // appended to a text file ("prec mode class ipt js tj gsplit x2 ms" per line), so a tuned
 // shape is reused by later runs.  x2 = 1 selects the packed f32x2 sweep (pn_pair2.cuh).
@@ -114,7 +116,9 @@ std::vector<PairCfg> tune_candidates(bool f32, int mode, int nstar, int sms) {
                 if (g > 1 && g > ntiles / 4) break;  // keep >= 4 tiles per j-range
                 c.gsplit = g;
                 c.x2 = 0;
-                out.push_back(c);
+                // large mixed-precision systems: the packed sweep only (the scalar one measured
+                // 15-20 % slower there at every shape)
+                if (!(f32 && big)) out.push_back(c);
                 if (f32 && js == 1 && ipt <= 2) {  // the packed f32x2 sweep of the same shape
                     c.x2 = 1;
                     out.push_back(c);
