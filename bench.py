@@ -613,7 +613,10 @@ def headline(args, rank, world, dist):
         # step's time outside the three pair sweeps, against the measured HBM copy bandwidth
         on_ms = max(float(step_ms.mean()) - float(pair_ms.mean()), 0.0) / 3.0
         gs = st.grid_split
-        moved = 216 + 56 + 72 * gs + 168  # prep in/out; finish: per-star data, split sums, stage state
+        # k_prep reads x, v, m (56 B) and writes spos, the paired pack, the i-side pack (96 B; the
+        # scalar pack's 64 B too when the scalar sweep runs); k_finish reads v, m, spos (56 B) and
+        # the j-range partial sums (9 doubles per split), and reads/writes the stage state (168 B)
+        moved = 56 + (96 if st.pair_variant in (2, 3) else 160) + 56 + 72 * gs + 168
         algo = 104 + 144                  # BH-star O(N) terms + one stage update, per star
         peak_hbm = _measured_hbm_gbs()
         line["o_n_kernels"] = {"ms_per_evaluation": on_ms, "bytes_per_star_moved": moved,

@@ -148,11 +148,13 @@ __device__ __forceinline__ void prep_body(const PrepArgs &a, int blk, int nblk) 
                 hi[k] = (float)r;
                 lo[k] = (float)(r - (double)hi[k]);
             }
-            float4 *pk = static_cast<float4 *>(a.pack);
-            pk[j] = make_float4(hi[0], hi[1], hi[2], (float)mj);
-            pk[a.npad + j] = make_float4(lo[0], lo[1], lo[2], (float)mu3);
-            pk[2 * a.npad + j] = make_float4((float)vv[0], (float)vv[1], (float)vv[2], (float)qe);
-            pk[3 * a.npad + j] = make_float4((float)c1, (float)c3, (float)k35, 0.f);
+            if (a.pack) {  // the scalar sweep's pack (not needed when only the packed sweep runs)
+                float4 *pk = static_cast<float4 *>(a.pack);
+                pk[j] = make_float4(hi[0], hi[1], hi[2], (float)mj);
+                pk[a.npad + j] = make_float4(lo[0], lo[1], lo[2], (float)mu3);
+                pk[2 * a.npad + j] = make_float4((float)vv[0], (float)vv[1], (float)vv[2], (float)qe);
+                pk[3 * a.npad + j] = make_float4((float)c1, (float)c3, (float)k35, 0.f);
+            }
             if (a.pack2) {  // paired layout: star j is lane (j & 1) of pair j / 2; scaled
                 const int lane = j & 1;
                 const size_t prow = (size_t)a.npad / 2;
@@ -291,6 +293,14 @@ __device__ __forceinline__ void finish_body(const FinishArgs &a, int blk, int nb
             double t = 0.0;
             for (int g = 0; g < a.gsplit; ++g) t += a.acc[((size_t)g * a.nacc + k) * a.npad + i];
             S[k] = t;
+        }
+        if (a.self_fp64 && nk > A_U) {
+            // the self pair (d = 0, Q = 1/eps) of S0 and U, left out of the FP32 sums: its terms
+            // can exceed the rest of those sums by orders of magnitude, and the reference's
+            // removal below must cancel them exactly
+            const double qs = 1.0 / sqrt(eps2);
+            S[A_S0] += mi * (qs * qs * qs);
+            S[A_U] += (mi * R3) * qs;
         }
         if (a.sums_out)
             for (int k = 0; k < nk; ++k) a.sums_out[(size_t)k * a.npad + i] = S[k];

@@ -315,17 +315,16 @@ def test_mixed_error_plummer(pn):
             assert np.sqrt((d ** 2).mean() / (np.linalg.norm(a64, axis=1) ** 2).mean()) <= 1e-6
 
 
-def test_mixed_error_bound_per_particle_at_c1(pn):
+def test_mixed_error_per_particle_at_c1(pn):
     """Mixed precision at the reference's c = 1, particle by particle (N = 16,384 Plummer + BH).
 
     There the 1PN part of a star's acceleration is as large as its Newtonian part and cancels it
-    on some stars, so |a_i| can be far below the magnitude of what is summed for it.  The FP32
-    pair sums are accurate relative to that magnitude, so the bound is stated against it:
-        |a32_i - a64_i| <= 5e-6 (|aN_i| + |aPN_i|),
-    aN = the Newtonian force (inv_c2 = 0), aPN = a - aN, both from the FP64 path; equivalently
-    the relative error is at most 5e-6 kappa_i with kappa_i = (|aN_i| + |aPN_i|) / |a_i|.  The
-    RMS of the error over that magnitude must stay at FP32 rounding (<= 1e-7), and so must the
-    per-particle RMS relative error of the stars whose kappa_i is below 10."""
+    on some stars.  The FP32 sweep leaves each star's self pair out of the S0 and U sums and the
+    finishing kernel adds it in FP64 (its terms m/eps^3 and m R^3/eps can exceed the rest of those
+    sums by orders of magnitude, and the reference's self-pair removal cancels them), so the
+    per-particle relative error stays at FP32 rounding: RMS <= 1e-6, and every particle within
+    5e-6 of the magnitude of its two parts, |a32_i - a64_i| <= 5e-6 (|aN_i| + |aPN_i|) with
+    aN the Newtonian force (inv_c2 = 0) and aPN = a - aN, both from the FP64 path."""
     n = 16384
     s = pn.config_plummer(n, 9)
     eps = pn.plummer_eps(n)
@@ -335,15 +334,14 @@ def test_mixed_error_bound_per_particle_at_c1(pn):
     scale = np.linalg.norm(aN, axis=1) + np.linalg.norm(a64 - aN, axis=1)
     err = np.linalg.norm(a32 - a64, axis=1)
     na = np.linalg.norm(a64, axis=1)
-    kappa = scale / na
+    rel = err / na
     r = err / scale
-    worst = int(np.argmax(r))
-    info = (float(r.max()), worst, float(kappa[worst]), float(kappa.max()), float(np.sqrt((r ** 2).mean())))
+    worst = int(np.argmax(rel))
+    info = {"rms_rel": float(np.sqrt((rel ** 2).mean())), "max_rel": float(rel.max()),
+            "worst": worst, "kappa_worst": float(scale[worst] / na[worst]),
+            "bh_dist_worst": float(np.linalg.norm(s.x[worst] - s.x[0])), "max_err_over_parts": float(r.max())}
+    assert np.sqrt((rel ** 2).mean()) <= 1e-6, info
     assert r.max() <= 5e-6, info
-    assert np.sqrt((r ** 2).mean()) <= 1e-7, info
-    well = kappa < 10
-    e = err[well] / na[well]
-    assert np.sqrt((e ** 2).mean()) <= 1e-6, (float(np.sqrt((e ** 2).mean())), info)
 
 
 def test_mixed_energy_drift_matches_fp64(pn):
