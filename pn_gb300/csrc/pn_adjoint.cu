@@ -510,22 +510,28 @@ __global__ void __launch_bounds__(VJP_NT) k_pair_vjp(const PairVjpArgs a) {
 // skipped (its mu3 term is added per row, as in the ordered sweep).
 constexpr int SYM_T = 128;
 
-template <typename T> constexpr int sym_min_blocks() { return sizeof(T) == 4 ? 4 : 2; }
+// Rows per lane: FP32 lanes hold two rows p against the same q (the q data read from shared
+// memory and the 17 shuffles of q's sums then serve two pairs), FP64 lanes one (register-bound).
+template <typename T> __host__ __device__ constexpr int sym_rows() { return sizeof(T) == 4 ? 2 : 1; }
+template <typename T> __host__ __device__ constexpr int sym_threads() { return SYM_T / sym_rows<T>(); }
+template <typename T> __host__ __device__ constexpr int sym_min_blocks() { return sizeof(T) == 4 ? 6 : 2; }
 
 template <typename T>
 constexpr size_t sym_smem_bytes() {
     return (size_t)(VjpPack<T>::NGF + VjpPack<T>::NGA) * SYM_T * sizeof(typename VjpPack<T>::V) +
-           (size_t)4 * NY * SYM_T * sizeof(T);
+           (size_t)(sym_threads<T>() / 32) * NY * SYM_T * sizeof(T);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(SYM_T, (sym_min_blocks<T>())) k_pair_vjp_sym(const PairVjpArgs a, T *part) {
+__global__ void __launch_bounds__(sym_threads<T>(), (sym_min_blocks<T>()))
+    k_pair_vjp_sym(const PairVjpArgs a, T *part) {
     using V = typename VjpPack<T>::V;
     constexpr int NGF = VjpPack<T>::NGF, NGA = VjpPack<T>::NGA;
+    constexpr int R = sym_rows<T>(), NTH = sym_threads<T>(), NW = NTH / 32;
     constexpr bool F32 = sizeof(T) == 4;
     extern __shared__ __align__(128) unsigned char smem[];
     V *qd = reinterpret_cast<V *>(smem);                                          // [NGF + NGA][SYM_T]
-    T *qp = reinterpret_cast<T *>(smem + (size_t)(NGF + NGA) * SYM_T * sizeof(V));  // [4][NY][SYM_T]
+    T *qp = reinterpret_cast<T *>(smem + (size_t)(NGF + NGA) * SYM_T * sizeof(V));  // [NW][NY][SYM_T]
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // work item u -> tile pair (I, J), I <= J, u = J (J + 1) / 2 + I
     const long long u = blockIdx.x;
@@ -537,26 +543,35 @@ __global__ void __launch_bounds__(SYM_T, (sym_min_blocks<T>())) k_pair_vjp_sym(c
     const V *pf = static_cast<const V *>(a.pack);
     const V *pa = static_cast<const V *>(a.apack);
     const int q0 = J * SYM_T;
+    for (int e = tid; e < SYM_T; e += NTH) {
 #pragma unroll
-    for (int g = 0; g < NGF; ++g) qd[g * SYM_T + tid] = pf[(size_t)g * a.npad + q0 + tid];
+        for (int g = 0; g < NGF; ++g) qd[g * SYM_T + e] = pf[(size_t)g * a.npad + q0 + e];
 #pragma unroll
-    for (int g = 0; g < NGA; ++g) qd[(NGF + g) * SYM_T + tid] = pa[(size_t)g * a.npad + q0 + tid];
-    const int p = I * SYM_T + tid;
-    VjpState<T> P;
-    vjp_load<T>(P, pf, pa, a.npad, p);
-    if constexpr (F32) {  // p relative to tile J's origin, as an FP32 hi/lo pair
-        const TileOrigin o = a.torg[J];
-        const double rx = a.spos[p] - o.x, ry = a.spos[a.npad + p] - o.y, rz = a.spos[2 * a.npad + p] - o.z;
-        P.ex = (float)rx; P.ey = (float)ry; P.ez = (float)rz;
-        P.lx = (float)(rx - (double)P.ex); P.ly = (float)(ry - (double)P.ey); P.lz = (float)(rz - (double)P.ez);
+        for (int g = 0; g < NGA; ++g) qd[(NGF + g) * SYM_T + e] = pa[(size_t)g * a.npad + q0 + e];
     }
-    T y[NY], z[NY];
+    // lane's rows: local star 32 (R warp + r) + lane of tile I
+    VjpState<T> P[R];
+    T y[R][NY];
 #pragma unroll
-    for (int c = 0; c < NY; ++c) y[c] = T(0);
+    for (int r = 0; r < R; ++r) {
+        const int p = I * SYM_T + 32 * (R * warp + r) + lane;
+        vjp_load<T>(P[r], pf, pa, a.npad, p);
+        if constexpr (F32) {  // p relative to tile J's origin, as an FP32 hi/lo pair
+            const TileOrigin o = a.torg[J];
+            const double rx = a.spos[p] - o.x, ry = a.spos[a.npad + p] - o.y, rz = a.spos[2 * a.npad + p] - o.z;
+            P[r].ex = (float)rx; P[r].ey = (float)ry; P[r].ez = (float)rz;
+            P[r].lx = (float)(rx - (double)P[r].ex);
+            P[r].ly = (float)(ry - (double)P[r].ey);
+            P[r].lz = (float)(rz - (double)P[r].ez);
+        }
+#pragma unroll
+        for (int c = 0; c < NY; ++c) y[r][c] = T(0);
+    }
     __syncthreads();
     const T eps2 = (T)a.eps2;
     const V *qa = qd + NGF * SYM_T;
     const int from = (lane + 1) & 31;
+    T z[NY];
     for (int k = 0; k < SYM_T / 32; ++k) {
 #pragma unroll
         for (int c = 0; c < NY; ++c) z[c] = T(0);
@@ -565,19 +580,22 @@ __global__ void __launch_bounds__(SYM_T, (sym_min_blocks<T>())) k_pair_vjp_sym(c
             const int qi = k * 32 + ((lane + st) & 31);
             VjpState<T> Qj;
             vjp_load<T>(Qj, qd, qa, SYM_T, qi);
-            T dx, dy, dz;
-            if constexpr (F32) {
-                dx = (Qj.ex - P.ex) + (Qj.lx - P.lx);
-                dy = (Qj.ey - P.ey) + (Qj.ly - P.ly);
-                dz = (Qj.ez - P.ez) + (Qj.lz - P.lz);
-            } else {
-                dx = Qj.ex - P.ex;
-                dy = Qj.ey - P.ey;
-                dz = Qj.ez - P.ez;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                T dx, dy, dz;
+                if constexpr (F32) {
+                    dx = (Qj.ex - P[r].ex) + (Qj.lx - P[r].lx);
+                    dy = (Qj.ey - P[r].ey) + (Qj.ly - P[r].ly);
+                    dz = (Qj.ez - P[r].ez) + (Qj.lz - P[r].lz);
+                } else {
+                    dx = Qj.ex - P[r].ex;
+                    dy = Qj.ey - P[r].ey;
+                    dz = Qj.ez - P[r].ez;
+                }
+                const VjpTerms<T> t = vjp_terms<T>(P[r], Qj, dx, dy, dz, eps2, diag && k == R * warp + r && st == 0);
+                vjp_acc_p<T>(y[r], t, Qj, dx, dy, dz);
+                vjp_acc_q<T>(z, t, P[r], dx, dy, dz);
             }
-            const VjpTerms<T> r = vjp_terms<T>(P, Qj, dx, dy, dz, eps2, diag && k == warp && st == 0);
-            vjp_acc_p<T>(y, r, Qj, dx, dy, dz);
-            vjp_acc_q<T>(z, r, P, dx, dy, dz);
 #pragma unroll
             for (int c = 0; c < NY; ++c) z[c] = __shfl_sync(0xffffffffu, z[c], from);
         }
@@ -585,31 +603,56 @@ __global__ void __launch_bounds__(SYM_T, (sym_min_blocks<T>())) k_pair_vjp_sym(c
         for (int c = 0; c < NY; ++c) qp[(warp * NY + c) * SYM_T + k * 32 + lane] = z[c];
     }
     __syncthreads();
-    const int q = q0 + tid;
+    // rows q of tile J: the warps' sums added in a fixed order; one thread per star q
+    for (int e = tid; e < SYM_T; e += NTH) {
 #pragma unroll
-    for (int c = 0; c < NY; ++c) {
-        const T zq = ((qp[c * SYM_T + tid] + qp[(NY + c) * SYM_T + tid]) + qp[(2 * NY + c) * SYM_T + tid]) +
-                     qp[(3 * NY + c) * SYM_T + tid];
-        if (diag) {
-            part[((size_t)I * NY + c) * a.npad + p] = T(0.5) * (y[c] + zq);
-        } else {
-            part[((size_t)J * NY + c) * a.npad + p] = y[c];   // row p, its pairs with tile J
-            part[((size_t)I * NY + c) * a.npad + q] = zq;     // row q, its pairs with tile I
+        for (int c = 0; c < NY; ++c) {
+            T zq = qp[c * SYM_T + e];
+#pragma unroll
+            for (int w = 1; w < NW; ++w) zq += qp[(w * NY + c) * SYM_T + e];
+            if (diag)
+                qp[c * SYM_T + e] = zq;  // this thread alone reads and writes star e's slots
+            else
+                part[((size_t)I * NY + c) * a.npad + q0 + e] = zq;  // row q, its pairs with tile I
+        }
+    }
+    if (diag) __syncthreads();  // uniform over the CTA
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int pl = 32 * (R * warp + r) + lane;
+        const int p = I * SYM_T + pl;
+#pragma unroll
+        for (int c = 0; c < NY; ++c) {
+            if (diag)  // every pair of the tile was visited in both orders: half of each
+                part[((size_t)I * NY + c) * a.npad + p] = T(0.5) * (y[r][c] + qp[c * SYM_T + pl]);
+            else
+                part[((size_t)J * NY + c) * a.npad + p] = y[r][c];  // row p, its pairs with tile J
         }
     }
 }
 
-// Per star: its sums over every tile (FP64, tile order) and the row outputs (split 0 of out).
+// Per (star, sum): the star's slots over every tile, added in tile order in FP64.
 template <typename T>
-__global__ void __launch_bounds__(128) k_vjp_sym_rows(const PairVjpArgs a, const T *part, int nt) {
+__global__ void __launch_bounds__(256) k_vjp_sym_reduce(const T *part, double *Y, int nt, int nstar, int npad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (i >= nstar) return;
+    const T *src = part + (size_t)c * npad + i;
+    const size_t stride = (size_t)NY * npad;
+    double t = 0.0;
+#pragma unroll 8
+    for (int b = 0; b < nt; ++b) t += (double)src[(size_t)b * stride];
+    Y[(size_t)c * npad + i] = t;
+}
+
+// Per star: the row outputs (split 0 of out) from its summed slots.
+template <typename T>
+__global__ void __launch_bounds__(128) k_vjp_sym_rows(const PairVjpArgs a, const double *Ysum) {
     using V = typename VjpPack<T>::V;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.nstar) return;
     double Y[NY];
-    for (int c = 0; c < NY; ++c) Y[c] = 0.0;
-    for (int b = 0; b < nt; ++b)
-#pragma unroll
-        for (int c = 0; c < NY; ++c) Y[c] += (double)part[((size_t)b * NY + c) * a.npad + i];
+    for (int c = 0; c < NY; ++c) Y[c] = Ysum[(size_t)c * a.npad + i];
     VjpState<T> P;
     vjp_load<T>(P, static_cast<const V *>(a.pack), static_cast<const V *>(a.apack), a.npad, i);
     double o[NV_VJP];
@@ -752,6 +795,7 @@ struct AdjointWork {
     int vjp_splits = 0;
     int g_best = 1, g_nstar = -1, g_f32 = -1;  // split count of the ordered VJP sweep for this size
     void *sympart = nullptr;  // [tiles][NY][npad] partial sums of the symmetric sweep
+    double *symsum = nullptr; // [NY][npad] their sums over the tiles
     size_t sym_bytes = 0;
     double *m0bar = nullptr;
     unsigned *tickets = nullptr;
@@ -771,7 +815,7 @@ void free_adjoint(pn_ctx *c) {
     AdjointWork *w = c->adj;
     if (!w) return;
     void *b[] = {w->sums, w->apack, w->sdir, w->vdir, w->vjp, w->gbar, w->part, w->m0bar, w->tickets,
-                 w->work, w->ckpt, w->seg, w->segsums, w->sympart};
+                 w->work, w->ckpt, w->seg, w->segsums, w->sympart, w->symsum};
     for (void *p : b)
         if (p) cudaFree(p);
     delete w;
@@ -868,6 +912,12 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
             }
             w->sym_bytes = sym_bytes;
         }
+        if (!w->symsum) {
+            if (cudaMalloc(&w->symsum, (size_t)NY * c->npad * sizeof(double)) != cudaSuccess) {
+                cudaGetLastError();
+                return set_err(PN_ERR_NOMEM, "vjp row sums");
+            }
+        }
     } else {
         const int nib = (nstar + VJP_NT - 1) / VJP_NT;
         // j-range splits: the count whose CTAs fill the resident slots in the fewest tile-times,
@@ -913,6 +963,7 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
         if (sym) {
             const unsigned items = (unsigned)((long long)nt_sym * (nt_sym + 1) / 2);
             const unsigned nbr = (unsigned)((nstar + 127) / 128);
+            const unsigned nbsum = (unsigned)((nstar + 255) / 256);
             if (f32) {
                 const size_t smem = sym_smem_bytes<float>();
                 static size_t configured = 0;
@@ -920,9 +971,12 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
                     CU(cudaFuncSetAttribute(k_pair_vjp_sym<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
                     configured = smem;
                 }
-                k_pair_vjp_sym<float><<<items, SYM_T, smem, s>>>(qa, static_cast<float *>(w->sympart));
+                k_pair_vjp_sym<float><<<items, sym_threads<float>(), smem, s>>>(qa, static_cast<float *>(w->sympart));
                 CU(cudaGetLastError());
-                k_vjp_sym_rows<float><<<nbr, 128, 0, s>>>(qa, static_cast<const float *>(w->sympart), nt_sym);
+                k_vjp_sym_reduce<float><<<dim3(nbsum, NY), 256, 0, s>>>(static_cast<const float *>(w->sympart),
+                                                                       w->symsum, nt_sym, nstar, c->npad);
+                CU(cudaGetLastError());
+                k_vjp_sym_rows<float><<<nbr, 128, 0, s>>>(qa, w->symsum);
             } else {
                 const size_t smem = sym_smem_bytes<double>();
                 static size_t configured = 0;
@@ -930,9 +984,12 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
                     CU(cudaFuncSetAttribute(k_pair_vjp_sym<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
                     configured = smem;
                 }
-                k_pair_vjp_sym<double><<<items, SYM_T, smem, s>>>(qa, static_cast<double *>(w->sympart));
+                k_pair_vjp_sym<double><<<items, sym_threads<double>(), smem, s>>>(qa, static_cast<double *>(w->sympart));
                 CU(cudaGetLastError());
-                k_vjp_sym_rows<double><<<nbr, 128, 0, s>>>(qa, static_cast<const double *>(w->sympart), nt_sym);
+                k_vjp_sym_reduce<double><<<dim3(nbsum, NY), 256, 0, s>>>(static_cast<const double *>(w->sympart),
+                                                                        w->symsum, nt_sym, nstar, c->npad);
+                CU(cudaGetLastError());
+                k_vjp_sym_rows<double><<<nbr, 128, 0, s>>>(qa, w->symsum);
             }
             CU(cudaGetLastError());
         } else {
