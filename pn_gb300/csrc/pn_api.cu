@@ -354,7 +354,6 @@ int pn::eval_force(pn_ctx *c, const double *x, const double *v, const double *m,
     fa.spos = c->spos; fa.acc = c->acc; fa.glob = c->glob;
     fa.nstar = nstar; fa.npad = c->npad; fa.nacc = pair_nacc(mode); fa.gsplit = k.gsplit;
     fa.pn1 = mode_has_force(mode) && c->p.inv_c2 != 0.0;
-    fa.self_fp64 = is_f32(c) && mode_has_force(mode);
     fa.eps = c->p.eps; fa.eps2 = eps2; fa.inv_c2 = c->p.inv_c2; fa.dt = c->p.dt;
     fa.a = a_out; fa.asp = asp; fa.ask = ask;
     fa.stage = stage; fa.st = c->st; fa.ld = c->ld; fa.sums_out = sums_out;

@@ -186,14 +186,10 @@ template <typename T> __device__ __forceinline__ T pn_fma(T a, T b, T c);
 template <> __device__ __forceinline__ float pn_fma<float>(float a, float b, float c) { return fmaf(a, b, c); }
 template <> __device__ __forceinline__ double pn_fma<double>(double a, double b, double c) { return fma(a, b, c); }
 
-// MASK (FP32 force sweeps, tiles that hold the i-particle itself): keep = 0 drops the pair from
-// the S0 and U sums.  The self pair's S0 term m_i / eps^3 and U term m_i R_i^3 / eps can exceed
-// the rest of those sums by orders of magnitude (stars near the BH), so its FP32 rounding would
-// survive the reference's self-pair removal; the finishing kernel adds both in FP64 instead.
-template <int MODE, typename T, bool MASK = false>
+template <int MODE, typename T>
 __device__ __forceinline__ void pair_accumulate(T *acc, const IState<T> &I, T jx, T jy, T jz,
                                                 T jlx, T jly, T jlz, T jm, T jvx, T jvy, T jvz,
-                                                T jmu3, T jc1, T jc3, T jk35, T eps2, T keep = T(1)) {
+                                                T jmu3, T jc1, T jc3, T jk35, T eps2) {
     T dx, dy, dz;
     if constexpr (sizeof(T) == 4) {
         dx = (jx - I.ex) + (jlx - I.lx);
@@ -219,13 +215,8 @@ __device__ __forceinline__ void pair_accumulate(T *acc, const IState<T> &I, T jx
         acc[A_GY] = pn_fma(mQ3, dy, acc[A_GY]);
         acc[A_GZ] = pn_fma(mQ3, dz, acc[A_GZ]);
         acc[A_PHI] += mQ;
-        if constexpr (MASK) {
-            acc[A_S0] = pn_fma(keep, mQ3, acc[A_S0]);
-            acc[A_U] = pn_fma(jmu3 * keep, Q, acc[A_U]);
-        } else {
-            acc[A_S0] += mQ3;
-            acc[A_U] = pn_fma(jmu3, Q, acc[A_U]);
-        }
+        acc[A_S0] += mQ3;
+        acc[A_U] = pn_fma(jmu3, Q, acc[A_U]);
         const T dvx = jvx - I.vx, dvy = jvy - I.vy, dvz = jvz - I.vz;
         const T dv2 = pn_fma(dvz, dvz, pn_fma(dvy, dvy, dvx * dvx));
         const T vdj = pn_fma(jvz, dz, pn_fma(jvy, dy, jvx * dx));

@@ -214,7 +214,6 @@ static int ens_build_tables(pn_ens *e) {
             fa.nacc = pair_nacc(mode);
             fa.gsplit = g;
             fa.pn1 = mode == MODE_FORCE;
-            fa.self_fp64 = f32 && mode == MODE_FORCE;
             fa.eps = eps;
             fa.eps2 = eps2;
             fa.inv_c2 = e->p.inv_c2;

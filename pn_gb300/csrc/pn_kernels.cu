@@ -294,14 +294,6 @@ __device__ __forceinline__ void finish_body(const FinishArgs &a, int blk, int nb
             for (int g = 0; g < a.gsplit; ++g) t += a.acc[((size_t)g * a.nacc + k) * a.npad + i];
             S[k] = t;
         }
-        if (a.self_fp64 && nk > A_U) {
-            // the self pair (d = 0, Q = 1/eps) of S0 and U, left out of the FP32 sums: its terms
-            // can exceed the rest of those sums by orders of magnitude, and the reference's
-            // removal below must cancel them exactly
-            const double qs = 1.0 / sqrt(eps2);
-            S[A_S0] += mi * (qs * qs * qs);
-            S[A_U] += (mi * R3) * qs;
-        }
         if (a.sums_out)
             for (int k = 0; k < nk; ++k) a.sums_out[(size_t)k * a.npad + i] = S[k];
         const double Gv[3] = {S[A_GX], S[A_GY], S[A_GZ]};

@@ -44,7 +44,6 @@ struct FinishArgs {
     const double *spos, *acc, *glob;
     int nstar, npad, nacc, gsplit;
     int pn1;              // 1PN terms on (pair sweep in MODE_FORCE)
-    int self_fp64;        // the FP32 sweep left each star's self pair out of S0 and U: add it in FP64
     double eps, eps2, inv_c2, dt;
     double *a;            // output acceleration (may be null), [p*asp + k*ask]
     long long asp, ask;

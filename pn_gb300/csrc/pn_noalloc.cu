@@ -186,7 +186,6 @@ extern "C" int pn_force_noalloc(int n, const double *d_x, const double *d_v, con
     fa.spos = spos; fa.acc = acc; fa.glob = glob;
     fa.nstar = nstar; fa.npad = kNpad; fa.nacc = pair_nacc(mode); fa.gsplit = k.gsplit;
     fa.pn1 = mode == MODE_FORCE;
-    fa.self_fp64 = f32 && mode == MODE_FORCE;
     fa.eps = eps; fa.eps2 = eps2; fa.inv_c2 = inv_c2; fa.dt = 0.0;
     fa.a = d_a; fa.asp = 3; fa.ask = 1; fa.stage = 0;
     fa.part = part + (size_t)kBlocks * 8;

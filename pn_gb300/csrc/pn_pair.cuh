@@ -23,8 +23,6 @@
 // and returns.
 #pragma once
 
-#include <type_traits>
-
 #include "pn_device.cuh"
 
 namespace pn {
@@ -173,10 +171,6 @@ __device__ __forceinline__ bool pair_block(const PairArgs &a, int ibase, int spl
 #pragma unroll
             for (int q = 0; q < NACC; ++q) tacc[k][q] = T(0);
 
-        // FP32 force sweeps: the tile that holds this block's own stars masks each star's self
-        // pair out of S0 and U (pair_accumulate)
-        auto jloop = [&](auto masked) {
-            constexpr bool M = decltype(masked)::value;
 #pragma unroll 2
         for (int j = sub; j < tj; j += JS) {
             T jx, jy, jz, jm, jlx = 0, jly = 0, jlz = 0, jvx = 0, jvy = 0, jvz = 0, jmu3 = 0,
@@ -207,23 +201,14 @@ __device__ __forceinline__ bool pair_block(const PairArgs &a, int ibase, int spl
             }
 #pragma unroll
             for (int k = 0; k < IPT; ++k) {
-                if constexpr (F32) {
-                    T keep = T(1);
-                    if constexpr (M) keep = (ibase + grp + k * NI == t * tj + j) ? T(0) : T(1);
-                    pair_accumulate<MODE, T, M>(tacc[k], I[k], jx, jy, jz, jlx, jly, jlz, jm, jvx, jvy,
-                                                jvz, jmu3, jc1, jc3, jk35, eps2, keep);
-                } else {
+                if constexpr (F32)
+                    pair_accumulate<MODE, T>(tacc[k], I[k], jx, jy, jz, jlx, jly, jlz, jm, jvx, jvy,
+                                             jvz, jmu3, jc1, jc3, jk35, eps2);
+                else
                     pair_accumulate<MODE, T>(run[k], I[k], jx, jy, jz, jlx, jly, jlz, jm, jvx, jvy,
                                              jvz, jmu3, jc1, jc3, jk35, eps2);
-                }
             }
         }
-        };
-        const bool self_tile = F32 && mode_has_force(MODE) && t * tj < ibase + NI * IPT && (t + 1) * tj > ibase;
-        if (self_tile)
-            jloop(std::true_type{});
-        else
-            jloop(std::false_type{});
         if constexpr (F32) {
 #pragma unroll
             for (int k = 0; k < IPT; ++k)

@@ -22,8 +22,6 @@
 // that relative bias, a 1PN sub-term far below the FP32 rounding of the sums.
 #pragma once
 
-#include <type_traits>
-
 #include "pn_pair.cuh"
 
 namespace pn {
@@ -89,11 +87,10 @@ struct I2 {  // one i-particle, broadcast to both lanes
 };
 
 
-// MASK: keep (0 or 1 per lane) drops the i-particle's own pair from S0 and U (pair_accumulate).
-template <int MODE, bool MASK = false>
+template <int MODE>
 __device__ __forceinline__ void pair2_accumulate(f2 *acc, const I2 &I, f2 jx, f2 jy, f2 jz, f2 jlx, f2 jly,
                                                  f2 jlz, f2 jm, f2 jwx, f2 jwy, f2 jwz, f2 jmu3, f2 jc1,
-                                                 f2 jc3, f2 jk35, f2 eps2, f2 keep = 0ull) {
+                                                 f2 jc3, f2 jk35, f2 eps2) {
     const f2 dx = add2(sub2(jx, I.ex), sub2(jlx, I.lx));
     const f2 dy = add2(sub2(jy, I.ey), sub2(jly, I.ly));
     const f2 dz = add2(sub2(jz, I.ez), sub2(jlz, I.lz));
@@ -113,13 +110,8 @@ __device__ __forceinline__ void pair2_accumulate(f2 *acc, const I2 &I, f2 jx, f2
         acc[A_GY] = fma2(mQ3, dy, acc[A_GY]);
         acc[A_GZ] = fma2(mQ3, dz, acc[A_GZ]);
         acc[A_PHI] = add2(acc[A_PHI], mQ);
-        if constexpr (MASK) {
-            acc[A_S0] = fma2(keep, mQ3, acc[A_S0]);
-            acc[A_U] = fma2(mul2(jmu3, keep), Q, acc[A_U]);
-        } else {
-            acc[A_S0] = add2(acc[A_S0], mQ3);
-            acc[A_U] = fma2(jmu3, Q, acc[A_U]);
-        }
+        acc[A_S0] = add2(acc[A_S0], mQ3);
+        acc[A_U] = fma2(jmu3, Q, acc[A_U]);
         const f2 vivj = fma2(I.vz, jwz, fma2(I.vy, jwy, fma2(I.vx, jwx, I.nvi2)));  // 4 vi.vj - vi^2
         const f2 vdj = fma2(jwz, dz, fma2(jwy, dy, mul2(jwx, dx)));                // sqrt(3) vj.d
         const f2 vdi = fma2(I.vz, dz, fma2(I.vy, dy, mul2(I.vx, dx)));             // 4/sqrt(3) vi.d
@@ -281,38 +273,23 @@ __device__ __forceinline__ bool pair2_block(const PairArgs &a, int ibase, int sp
 #pragma unroll
             for (int q = 0; q < NTACC; ++q) tacc[k][q] = 0ull;  // +0.0f in both lanes
 
-        // the tile that holds this block's own stars masks each star's self pair out of S0 and U
-        auto jloop = [&](auto masked) {
-            constexpr bool M = decltype(masked)::value;
 #pragma unroll 2
-            for (int jp = 0; jp < tp; ++jp) {
-                f2 jx, jy, jz, jm, jlx, jly, jlz, jmu3, jvx = 0, jvy = 0, jvz = 0, jc1 = 0, jc3 = 0, jk35 = 0;  // scaled
-                lds2(b + jp, jx, jy);
-                lds2(b + tp + jp, jz, jm);
-                lds2(b + 2 * tp + jp, jlx, jly);
-                lds2(b + 3 * tp + jp, jlz, jmu3);
-                if constexpr (MODE != MODE_NEWTON) {
-                    lds2(b + 4 * tp + jp, jvx, jvy);
-                    lds2(b + 5 * tp + jp, jvz, jc1);
-                }
-                if constexpr (mode_has_force(MODE)) lds2(b + 6 * tp + jp, jc3, jk35);
-#pragma unroll
-                for (int k = 0; k < IPT; ++k) {
-                    f2 keep = 0ull;
-                    if constexpr (M) {
-                        const int rel = ibase + tid + k * NT - (t * tj + 2 * jp);  // i - j of lane 0
-                        keep = f2_pack(rel == 0 ? 0.f : 1.f, rel == 1 ? 0.f : 1.f);
-                    }
-                    pair2_accumulate<MODE, M>(tacc[k], I[k], jx, jy, jz, jlx, jly, jlz, jm, jvx, jvy, jvz, jmu3,
-                                              jc1, jc3, jk35, eps2, keep);
-                }
+        for (int jp = 0; jp < tp; ++jp) {
+            f2 jx, jy, jz, jm, jlx, jly, jlz, jmu3, jvx = 0, jvy = 0, jvz = 0, jc1 = 0, jc3 = 0, jk35 = 0;  // scaled
+            lds2(b + jp, jx, jy);
+            lds2(b + tp + jp, jz, jm);
+            lds2(b + 2 * tp + jp, jlx, jly);
+            lds2(b + 3 * tp + jp, jlz, jmu3);
+            if constexpr (MODE != MODE_NEWTON) {
+                lds2(b + 4 * tp + jp, jvx, jvy);
+                lds2(b + 5 * tp + jp, jvz, jc1);
             }
-        };
-        const bool self_tile = mode_has_force(MODE) && t * tj < ibase + NT * IPT && (t + 1) * tj > ibase;
-        if (self_tile)
-            jloop(std::true_type{});
-        else
-            jloop(std::false_type{});
+            if constexpr (mode_has_force(MODE)) lds2(b + 6 * tp + jp, jc3, jk35);
+#pragma unroll
+            for (int k = 0; k < IPT; ++k)
+                pair2_accumulate<MODE>(tacc[k], I[k], jx, jy, jz, jlx, jly, jlz, jm, jvx, jvy, jvz, jmu3, jc1,
+                                       jc3, jk35, eps2);
+        }
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
             float ts[NACC];
