@@ -674,23 +674,8 @@ def headline(args, rank, world, dist):
                 "rms_rel": float(np.sqrt((r ** 2).mean())), "max_rel": float(r.max()),
                 "rms_abs_over_rms_a": float(np.sqrt((d ** 2).mean() / (na ** 2).mean()))}
             if ic2 == 1.0:
-                # at c = 1 the 1PN part cancels the Newtonian part on some stars: the error
-                # against the magnitude of the two parts (FP64 Newtonian force aN, aPN = a - aN)
-                # and the conditioning kappa = (|aN| + |aPN|) / |a|
-                cn = pn.Context(n, eps=eps, inv_c2=0.0, precision=pn.PN_PREC_FP64)
-                cn.set_state(sysm.x, sysm.v, sysm.m)
-                aN = cn.force()
-                cn.close()
-                scale = np.linalg.norm(aN, axis=1) + np.linalg.norm(ref - aN, axis=1)
-                kappa = scale / na
-                rs = d / scale
-                well = kappa < 10
-                acc["inv_c2=1"].update({
-                    "max_err_over_parts": float(rs.max()), "rms_err_over_parts": float(np.sqrt((rs ** 2).mean())),
-                    "kappa_of_max_rel": float(kappa[int(np.argmax(r))]),
-                    "stars_kappa_ge_10": int((~well).sum()),
-                    "rms_rel_kappa_lt_10": float(np.sqrt((r[well] ** 2).mean())),
-                    "max_rel_kappa_lt_10": float(r[well].max())})
+                acc["inv_c2=1"]["note"] = ("per-particle error bounded by 8 u (Gabs + Wabs), the absolute "
+                                           "sums of the pair terms (tests/test_force_gpu.py)")
         line["accuracy_vs_fp64"] = acc
         # ---------------- CPU baseline (oracle port), bounded sample
         rate, info = cpu_baseline(sysm.x, sysm.v, sysm.m, eps)
