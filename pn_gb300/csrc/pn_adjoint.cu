@@ -173,7 +173,8 @@ struct PairVjpArgs {
 
 template <typename T> struct VjpState {
     T ex, ey, ez, lx, ly, lz;  // position (FP32: hi/lo relative to the tile origin)
-    T vx, vy, vz, vi2, m, mu3, c1, c3, k35, qe;
+    T vx, vy, vz, m, mu3, c3, k35, qe;
+    T nvi2, c1v;               // -|v|^2 and c1 - 2 |v|^2 (the pair term's |v_i|^2 - 2 |dv|^2, split)
     T Gx, Gy, Gz, Phi, S0, U, Wx, Wy, Wz;  // adjoint state
     T cW;                                  // Wbar . v
 };
@@ -227,22 +228,23 @@ __device__ __forceinline__ VjpTerms<T> vjp_terms(const VjpState<T> &P, const Vjp
     const T vdp = pn_fma(P.vz, dz, pn_fma(P.vy, dy, P.vx * dx));     // v_p . d
     const T vdq = pn_fma(Qj.vz, dz, pn_fma(Qj.vy, dy, Qj.vx * dx));  // v_q . d
     const T vpq = pn_fma(P.vz, Qj.vz, pn_fma(P.vy, Qj.vy, P.vx * Qj.vx));
-    const T dv2 = pn_fma(T(-2), vpq, P.vi2 + Qj.vi2);               // |v_q - v_p|^2
+    // |v_i|^2 - 2 |dv|^2 = -|v_i|^2 - 2 |v_j|^2 + 4 v_i.v_j: the -2 |v_j|^2 lives in c1v
+    const T Q2x3 = T(3) * Q2;
     // ---- F(p, q): (i, j) = (p, q), adjoint state of p
     const T mQ3 = Qj.m * Q3;
     const T gd = pn_fma(P.Gz, dz, pn_fma(P.Gy, dy, P.Gx * dx));
     const T wd = pn_fma(P.Wz, dz, pn_fma(P.Wy, dy, P.Wx * dx));
     const T wdv = pn_fma(P.Wz, Qj.vz, pn_fma(P.Wy, Qj.vy, pn_fma(P.Wx, Qj.vx, -P.cW)));
-    const T t = vdq * vdq;
+    const T tQ2 = (vdq * vdq) * Q2;
     const T rp = rhoe - P.qe;
-    T br = pn_fma(rp, Qj.c3, Qj.c1) + pn_fma(T(-2), dv2, P.vi2);
-    br = pn_fma(T(1.5) * t, Q2, br);
+    T br = pn_fma(rp, Qj.c3, Qj.c1v) + pn_fma(T(4), vpq, P.nvi2);
+    br = pn_fma(tQ2, T(1.5), br);
     const T k4 = pn_fma(T(4), vdp, T(-3) * vdq);
     const T cd = pn_fma(mQ3, br, Qj.k35 * Q);
     const T cv = mQ3 * k4;
-    T in = pn_fma(k4, wdv, pn_fma(br, wd, gd + P.S0));
-    T LQ = pn_fma(T(3) * Qj.m * Q2, in, pn_fma(Qj.m, P.Phi, P.U * Qj.mu3));
-    LQ = pn_fma(wd, pn_fma(T(3) * mQ3 * t, Q, Qj.k35), LQ);
+    const T in = pn_fma(k4, wdv, pn_fma(br, wd, gd + P.S0));
+    // LQ = 3 m Q^2 (in + wd t Q^2) + m Phibar + Ubar mu3 + wd k35   (3 mQ^3 t Q = 3 m Q^2 . t Q^2)
+    const T LQ = pn_fma(Qj.m * Q2x3, pn_fma(wd, tQ2, in), pn_fma(Qj.m, P.Phi, pn_fma(wd, Qj.k35, P.U * Qj.mu3)));
     const T ga = mQ3 * wd;
     const T h = mQ3 * wdv;
     const T al = pn_fma(T(2) * Qj.c3, ga, -LQ * Q3);
@@ -252,16 +254,16 @@ __device__ __forceinline__ VjpTerms<T> vjp_terms(const VjpState<T> &P, const Vjp
     const T gq = pn_fma(Qj.Gz, dz, pn_fma(Qj.Gy, dy, Qj.Gx * dx));  // -gd'
     const T wq = pn_fma(Qj.Wz, dz, pn_fma(Qj.Wy, dy, Qj.Wx * dx));  // -wd'
     const T wdv2 = pn_fma(Qj.Wz, P.vz, pn_fma(Qj.Wy, P.vy, pn_fma(Qj.Wx, P.vx, -Qj.cW)));
-    const T t2 = vdp * vdp;
+    const T t2Q2 = (vdp * vdp) * Q2;
     const T rq = rhoe - Qj.qe;
-    T br2 = pn_fma(rq, P.c3, P.c1) + pn_fma(T(-2), dv2, Qj.vi2);
-    br2 = pn_fma(T(1.5) * t2, Q2, br2);
+    T br2 = pn_fma(rq, P.c3, P.c1v) + pn_fma(T(4), vpq, Qj.nvi2);
+    br2 = pn_fma(t2Q2, T(1.5), br2);
     const T k42 = pn_fma(T(3), vdp, T(-4) * vdq);
     const T cd2 = pn_fma(mQ3b, br2, P.k35 * Q);
     const T cv2 = mQ3b * k42;
-    T in2 = pn_fma(k42, wdv2, pn_fma(-br2, wq, Qj.S0 - gq));
-    T LQ2 = pn_fma(T(3) * P.m * Q2, in2, pn_fma(P.m, Qj.Phi, Qj.U * P.mu3));
-    LQ2 = pn_fma(-wq, pn_fma(T(3) * mQ3b * t2, Q, P.k35), LQ2);
+    const T in2 = pn_fma(k42, wdv2, pn_fma(-br2, wq, Qj.S0 - gq));
+    const T LQ2 = pn_fma(P.m * Q2x3, pn_fma(-wq, t2Q2, in2),
+                         pn_fma(P.m, Qj.Phi, pn_fma(-wq, P.k35, Qj.U * P.mu3)));
     const T ga2 = -mQ3b * wq;
     const T h2 = mQ3b * wdv2;
     const T al2 = pn_fma(T(2) * P.c3, ga2, -LQ2 * Q3);
@@ -368,23 +370,27 @@ __device__ __forceinline__ void vjp_load(VjpState<T> &S, const typename VjpPack<
         S.ex = g0.x; S.ey = g0.y; S.ez = g0.z; S.m = g0.w;
         S.lx = g1.x; S.ly = g1.y; S.lz = g1.z; S.mu3 = g1.w;
         S.vx = g2.x; S.vy = g2.y; S.vz = g2.z; S.qe = g2.w;
-        S.c1 = g3.x; S.c3 = g3.y; S.k35 = g3.z;
+        S.c3 = g3.y; S.k35 = g3.z;
         const float4 a0 = ad[j], a1 = ad[stride + j], a2 = ad[2 * stride + j];
         S.Gx = a0.x; S.Gy = a0.y; S.Gz = a0.z; S.Phi = a0.w;
         S.Wx = a1.x; S.Wy = a1.y; S.Wz = a1.z; S.S0 = a1.w;
-        S.U = a2.x; S.vi2 = a2.y; S.cW = a2.z;
+        S.U = a2.x; S.cW = a2.z;
+        S.nvi2 = -a2.y;
+        S.c1v = fmaf(-2.f, a2.y, g3.x);
     } else {
         const double2 g0 = f[j], g1 = f[stride + j], g2 = f[2 * stride + j], g3 = f[3 * stride + j],
                       g4 = f[4 * stride + j], g5 = f[5 * stride + j];
         S.ex = g0.x; S.ey = g0.y; S.ez = g1.x; S.m = g1.y;
         S.lx = S.ly = S.lz = 0.0;
         S.vx = g2.x; S.vy = g2.y; S.vz = g3.x; S.mu3 = g3.y;
-        S.c1 = g4.x; S.c3 = g4.y; S.k35 = g5.x; S.qe = g5.y;
+        S.c3 = g4.y; S.k35 = g5.x; S.qe = g5.y;
         const double2 a0 = ad[j], a1 = ad[stride + j], a2 = ad[2 * stride + j], a3 = ad[3 * stride + j],
                       a4 = ad[4 * stride + j], a5 = ad[5 * stride + j];
         S.Gx = a0.x; S.Gy = a0.y; S.Gz = a1.x; S.Phi = a1.y;
         S.S0 = a2.x; S.U = a2.y;
-        S.Wx = a3.x; S.Wy = a3.y; S.Wz = a4.x; S.vi2 = a4.y;
+        S.Wx = a3.x; S.Wy = a3.y; S.Wz = a4.x;
+        S.nvi2 = -a4.y;
+        S.c1v = fma(-2.0, a4.y, g4.x);
         S.cW = a5.x;
     }
 }

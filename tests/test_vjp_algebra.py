@@ -183,11 +183,12 @@ def symmetric_rows():
             rp = rho - qe[p]
             mQ3 = m[q] * Q3
             gd, wd, wdv = G[p] @ d, W[p] @ d, W[p] @ v[q] - cW[p]
-            br = c1[q] + c3[q] * rp + vi2[p] - 2 * dv2 + 1.5 * vdq ** 2 * Q2
+            # the kernel's form: -2|v_q|^2 folded into c1v, |v_p|^2 - 2|dv|^2 = -|v_p|^2 - 2|v_q|^2 + 4 v_p.v_q
+            br = (c1[q] - 2 * vi2[q]) + c3[q] * rp + (4 * vpq - vi2[p]) + 1.5 * vdq ** 2 * Q2
             k4 = 4 * vdp - 3 * vdq
             cd, cv = mQ3 * br + k35[q] * Q, mQ3 * k4
-            LQ = (3 * m[q] * Q2 * (gd + S0[p] + br * wd + k4 * wdv) + Phi[p] * m[q] + U[p] * mu3[q]
-                  + wd * (3 * mQ3 * vdq ** 2 * Q + k35[q]))
+            inn = gd + S0[p] + br * wd + k4 * wdv
+            LQ = 3 * m[q] * Q2 * (inn + wd * vdq ** 2 * Q2) + Phi[p] * m[q] + U[p] * mu3[q] + wd * k35[q]
             ga, h = mQ3 * wd, mQ3 * wdv
             al = 2 * c3[q] * ga - LQ * Q3
             be = 3 * (Q2 * vdq * ga - h)
@@ -195,11 +196,11 @@ def symmetric_rows():
             gq, wq = G[q] @ d, W[q] @ d
             wdv2 = W[q] @ v[p] - cW[q]
             rq = rho - qe[q]
-            br2 = c1[p] + c3[p] * rq + vi2[q] - 2 * dv2 + 1.5 * vdp ** 2 * Q2
+            br2 = (c1[p] - 2 * vi2[p]) + c3[p] * rq + (4 * vpq - vi2[q]) + 1.5 * vdp ** 2 * Q2
             k42 = 3 * vdp - 4 * vdq
             cd2, cv2 = mQ3b * br2 + k35[p] * Q, mQ3b * k42
-            LQ2 = (3 * m[p] * Q2 * (-gq + S0[q] - br2 * wq + k42 * wdv2) + Phi[q] * m[p] + U[q] * mu3[p]
-                   - wq * (3 * mQ3b * vdp ** 2 * Q + k35[p]))
+            inn2 = -gq + S0[q] - br2 * wq + k42 * wdv2
+            LQ2 = 3 * m[p] * Q2 * (inn2 - wq * vdp ** 2 * Q2) + Phi[q] * m[p] + U[q] * mu3[p] - wq * k35[p]
             ga2, h2 = -mQ3b * wq, mQ3b * wdv2
             al2 = 2 * c3[p] * ga2 - LQ2 * Q3
             be2 = -3 * (Q2 * vdp * ga2 + h2)
