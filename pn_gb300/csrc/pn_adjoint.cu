@@ -40,7 +40,7 @@ enum GbarSlot : int { GB_A1 = 0, GB_B3X, GB_B3Y, GB_B3Z, GB_C, GB_PX, GB_PY, GB_
 
 // Threads per block of the O(N) adjoint kernels: their per-star FP64 work is heavy, so small
 // blocks spread a system of a few thousand stars over every SM.
-constexpr int VJP_ON_NT = 64;
+constexpr int VJP_ON_NT = 32;
 
 // ------------------------------------------------------------------ per-star adjoint
 struct FinVjpArgs {
@@ -637,18 +637,37 @@ __global__ void __launch_bounds__(sym_threads<T>(), (sym_min_blocks<T>()))
     }
 }
 
-// Per (star, sum): the star's slots over every tile, added in tile order in FP64.
+// Per (star, sum): the star's slots over every tile, added in tile order in FP64.  Each thread
+// takes 16 bytes of consecutive stars (4 in FP32, 2 in FP64) with one vector load per tile, so
+// that enough bytes are in flight to stream the partial sums at HBM/L2 rate.
+template <typename T> struct SymVec;
+template <> struct SymVec<float> { using V = float4; static constexpr int W = 4; };
+template <> struct SymVec<double> { using V = double2; static constexpr int W = 2; };
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_vjp_sym_reduce(const T *part, double *Y, int nt, int nstar, int npad) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    using V = typename SymVec<T>::V;
+    constexpr int W = SymVec<T>::W;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) * W;  // first star of this thread
     const int c = blockIdx.y;
     if (i >= nstar) return;
-    const T *src = part + (size_t)c * npad + i;
-    const size_t stride = (size_t)NY * npad;
-    double t = 0.0;
+    const V *src = reinterpret_cast<const V *>(part + (size_t)c * npad + i);
+    const size_t stride = (size_t)NY * npad / W;  // one tile, in vectors
+    double t[W];
+#pragma unroll
+    for (int e = 0; e < W; ++e) t[e] = 0.0;
 #pragma unroll 8
-    for (int b = 0; b < nt; ++b) t += (double)src[(size_t)b * stride];
-    Y[(size_t)c * npad + i] = t;
+    for (int b = 0; b < nt; ++b) {
+        const V x = src[(size_t)b * stride];
+        if constexpr (W == 4) {
+            t[0] += (double)x.x; t[1] += (double)x.y; t[2] += (double)x.z; t[3] += (double)x.w;
+        } else {
+            t[0] += (double)x.x; t[1] += (double)x.y;
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < W; ++e)
+        if (i + e < nstar) Y[(size_t)c * npad + i + e] = t[e];
 }
 
 // Per star: the row outputs (split 0 of out) from its summed slots.
@@ -808,10 +827,18 @@ struct AdjointWork {
     double *work = nullptr;  // [12][3][ld]: Xb Vb xb vb x1b v1b x2b v2b ab xF vF spare
     // trajectory
     int nsteps = 0, K = 0, nck = 0;
-    double *ckpt = nullptr;     // [nck][6][ld]  (x, v at steps 0, K, 2K, ...)
-    double *seg = nullptr;      // [K][3][6][ld] evaluation states of a segment's stages
-    double *segsums = nullptr;  // [K][3][9][npad]
-    int seg_holds = -1;         // segment whose stages seg/segsums hold (-1: none)
+    double *ckpt = nullptr;        // [nck][6][ld]  (x, v at steps 0, K, 2K, ...)
+    double *seg[2] = {};           // [K][3][6][ld] evaluation states of a segment's stages (2 buffers)
+    double *segsums[2] = {};       // [K][3][9][npad]
+    int holds[2] = {-1, -1};       // segment whose stages each buffer holds (-1: none)
+    // the VJP's own copies of the evaluation buffers (pack, tile origins, BH-relative positions,
+    // global sums), so that a segment's recomputation (which uses the context's) can run on the
+    // second stream while the previous segment is reversed
+    void *vpack = nullptr;
+    TileOrigin *vtorg = nullptr;
+    double *vspos = nullptr, *vpart = nullptr, *vglob = nullptr;
+    cudaStream_t s2 = nullptr;     // recomputation stream
+    cudaEvent_t ev_rec[2] = {}, ev_done[2] = {}, ev_sync = nullptr;
     double time0 = 0.0;
 };
 
@@ -820,10 +847,18 @@ namespace pn {
 void free_adjoint(pn_ctx *c) {
     AdjointWork *w = c->adj;
     if (!w) return;
+    if (w->s2) cudaStreamSynchronize(w->s2);
     void *b[] = {w->sums, w->apack, w->sdir, w->vdir, w->vjp, w->gbar, w->part, w->m0bar, w->tickets,
-                 w->work, w->ckpt, w->seg, w->segsums, w->sympart, w->symsum};
+                 w->work, w->ckpt, w->seg[0], w->seg[1], w->segsums[0], w->segsums[1], w->sympart, w->symsum,
+                 w->vpack, w->vtorg, w->vspos, w->vpart, w->vglob};
     for (void *p : b)
         if (p) cudaFree(p);
+    for (int q = 0; q < 2; ++q) {
+        if (w->ev_rec[q]) cudaEventDestroy(w->ev_rec[q]);
+        if (w->ev_done[q]) cudaEventDestroy(w->ev_done[q]);
+    }
+    if (w->ev_sync) cudaEventDestroy(w->ev_sync);
+    if (w->s2) cudaStreamDestroy(w->s2);
     delete w;
     c->adj = nullptr;
 }
@@ -848,11 +883,25 @@ static int adj_ensure(pn_ctx *c) {
                     mal((void **)&w->sdir, 3 * np * 8) && mal((void **)&w->vdir, 3 * np * 8) &&
                     mal((void **)&w->gbar, 16 * 8) && mal((void **)&w->part, (np / VJP_ON_NT + 2) * 16 * 8) &&
                     mal((void **)&w->m0bar, 2 * 8) && mal((void **)&w->tickets, 4 * sizeof(unsigned)) &&
-                    mal((void **)&w->work, 12 * 3 * ld * 8);
+                    mal((void **)&w->work, 12 * 3 * ld * 8) && mal(&w->vpack, 6 * np * 16) &&
+                    mal((void **)&w->vtorg, (np / 32 + 1) * sizeof(TileOrigin)) &&
+                    mal((void **)&w->vspos, 3 * np * 8) && mal((void **)&w->vpart, (np / 256 + 2) * 8 * 2 * 8) &&
+                    mal((void **)&w->vglob, 16 * 8);
     if (!ok) {
         free_adjoint(c);
         return set_err(PN_ERR_NOMEM, "adjoint buffers");
     }
+    bool ev_ok = cudaStreamCreateWithFlags(&w->s2, cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&w->ev_sync, cudaEventDisableTiming) == cudaSuccess;
+    for (int q = 0; q < 2 && ev_ok; ++q)
+        ev_ok = cudaEventCreateWithFlags(&w->ev_rec[q], cudaEventDisableTiming) == cudaSuccess &&
+                cudaEventCreateWithFlags(&w->ev_done[q], cudaEventDisableTiming) == cudaSuccess;
+    if (!ev_ok) {
+        cudaGetLastError();
+        free_adjoint(c);
+        return set_err(PN_ERR_CUDA, "adjoint streams");
+    }
+    CU(cudaMemset(w->vpack, 0, 6 * np * 16));
     CU(cudaMemset(w->tickets, 0, 4 * sizeof(unsigned)));
     CU(cudaMemset(w->apack, 0, 6 * np * 16));
     CU(cudaMemset(w->work, 0, 12 * 3 * ld * 8));
@@ -883,12 +932,12 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
     pa.x = x; pa.v = v; pa.m = c->st.m; pa.sp = 1; pa.sk = ld;
     pa.nstar = nstar; pa.npad = c->npad; pa.nfill = (int)round_up(nstar > 0 ? nstar : 1, 256);
     pa.tj = tj; pa.f32 = f32; pa.eps2 = eps2;
-    pa.pack = c->pack; pa.torg = c->torg; pa.spos = c->spos;
-    pa.part = c->part; pa.glob = c->glob; pa.ticket = &c->tickets[0];
+    pa.pack = w->vpack; pa.torg = w->vtorg; pa.spos = w->vspos;
+    pa.part = w->vpart; pa.glob = w->vglob; pa.ticket = &w->tickets[2];
     CU(launch_prep(pa, s));
     // per-star adjoint
     FinVjpArgs fa{};
-    fa.spos = c->spos; fa.v = v; fa.m = c->st.m; fa.sums = sums; fa.glob = c->glob;
+    fa.spos = w->vspos; fa.v = v; fa.m = c->st.m; fa.sums = sums; fa.glob = w->vglob;
     fa.vsp = 1; fa.vsk = ld; fa.abar = abar; fa.asp = 1; fa.ask = ld;
     fa.nstar = nstar; fa.npad = c->npad; fa.nfill = pa.nfill; fa.f32 = f32;
     fa.eps = c->p.eps; fa.eps2 = eps2; fa.ic2 = c->p.inv_c2;
@@ -963,13 +1012,13 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
     }
     if (nstar > 0) {
         PairVjpArgs qa{};
-        qa.pack = c->pack; qa.apack = w->apack; qa.torg = c->torg; qa.spos = c->spos; qa.out = w->vjp;
+        qa.pack = w->vpack; qa.apack = w->apack; qa.torg = w->vtorg; qa.spos = w->vspos; qa.out = w->vjp;
         qa.err = c->err; qa.nstar = nstar; qa.npad = c->npad; qa.tj = tj; qa.ntiles = ntiles; qa.gsplit = g;
         qa.eps2 = eps2;
         if (sym) {
             const unsigned items = (unsigned)((long long)nt_sym * (nt_sym + 1) / 2);
             const unsigned nbr = (unsigned)((nstar + 127) / 128);
-            const unsigned nbsum = (unsigned)((nstar + 255) / 256);
+            const unsigned nbsum = (unsigned)((nstar + 4 * 256 - 1) / (4 * 256));  // FP32: 4 stars per thread
             if (f32) {
                 const size_t smem = sym_smem_bytes<float>();
                 static size_t configured = 0;
@@ -992,7 +1041,7 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
                 }
                 k_pair_vjp_sym<double><<<items, sym_threads<double>(), smem, s>>>(qa, static_cast<double *>(w->sympart));
                 CU(cudaGetLastError());
-                k_vjp_sym_reduce<double><<<dim3(nbsum, NY), 256, 0, s>>>(static_cast<const double *>(w->sympart),
+                k_vjp_sym_reduce<double><<<dim3(2 * nbsum, NY), 256, 0, s>>>(static_cast<const double *>(w->sympart),
                                                                         w->symsum, nt_sym, nstar, c->npad);
                 CU(cudaGetLastError());
                 k_vjp_sym_rows<double><<<nbr, 128, 0, s>>>(qa, w->symsum);
@@ -1022,7 +1071,7 @@ static int vjp_eval(pn_ctx *c, const double *x, const double *v, const double *s
         }
     }
     AssembleArgs aa{};
-    aa.spos = c->spos; aa.m = c->st.m; aa.vjp = w->vjp; aa.sdir = w->sdir; aa.vdir = w->vdir; aa.gbar = w->gbar;
+    aa.spos = w->vspos; aa.m = c->st.m; aa.vjp = w->vjp; aa.sdir = w->sdir; aa.vdir = w->vdir; aa.gbar = w->gbar;
     aa.nstar = nstar; aa.npad = c->npad; aa.gsplit = nstar > 0 ? g : 0; aa.eps2 = eps2;
     aa.xbar = xbar; aa.vbar = vbar; aa.osp = 1; aa.osk = ld; aa.accumulate = accumulate;
     aa.m0_accumulate = m0_accumulate;
@@ -1070,18 +1119,17 @@ extern "C" int pn_force_vjp(pn_ctx *c, const double *abar, double *xbar, double 
     return PN_OK;
 }
 
-// `steps` integration steps from the context's current state, keeping every stage's evaluation
-// state and pair sums in seg/segsums (the same evaluations as pn_steps).
-static int record_segment(pn_ctx *c, int steps) {
+// `steps` integration steps from the context's current state on stream s, keeping every stage's
+// evaluation state and pair sums in segment buffer `buf` (the same evaluations as pn_steps).
+static int record_segment(pn_ctx *c, int steps, int buf, cudaStream_t s) {
     AdjointWork *w = c->adj;
     const size_t ld = (size_t)c->ld, np = (size_t)c->npad;
     const long long LD = c->ld;
-    cudaStream_t s = c->stream;
     for (int t = 0; t < steps; ++t) {
-        double *S0 = w->seg + ((size_t)t * 3 + 0) * 6 * ld;
-        double *S1 = w->seg + ((size_t)t * 3 + 1) * 6 * ld;
-        double *S2 = w->seg + ((size_t)t * 3 + 2) * 6 * ld;
-        double *ss = w->segsums + (size_t)t * 3 * 9 * np;
+        double *S0 = w->seg[buf] + ((size_t)t * 3 + 0) * 6 * ld;
+        double *S1 = w->seg[buf] + ((size_t)t * 3 + 1) * 6 * ld;
+        double *S2 = w->seg[buf] + ((size_t)t * 3 + 2) * 6 * ld;
+        double *ss = w->segsums[buf] + (size_t)t * 3 * 9 * np;
         CU(cudaMemcpyAsync(S0, c->st.x, 6 * ld * 8, cudaMemcpyDeviceToDevice, s));
         int rc = eval_force(c, c->st.x, c->st.v, c->st.m, 1, LD, nullptr, 3, 1, 1, s, false, -1, ss);
         if (rc) return rc;
@@ -1108,13 +1156,18 @@ extern "C" int pn_adj_forward(pn_ctx *c, int nsteps, int checkpoint_every) {
     const int K = checkpoint_every;
     const int nck = (nsteps + K - 1) / K;
     if (w->nsteps != nsteps || w->K != K) {
-        if (w->ckpt) cudaFree(w->ckpt);
-        if (w->seg) cudaFree(w->seg);
-        if (w->segsums) cudaFree(w->segsums);
-        w->ckpt = w->seg = w->segsums = nullptr;
-        if (cudaMalloc(&w->ckpt, (size_t)nck * 6 * ld * 8) != cudaSuccess ||
-            cudaMalloc(&w->seg, (size_t)K * 3 * 6 * ld * 8) != cudaSuccess ||
-            cudaMalloc(&w->segsums, (size_t)K * 3 * 9 * np * 8) != cudaSuccess) {
+        CU(cudaStreamSynchronize(w->s2));
+        void *old[] = {w->ckpt, w->seg[0], w->seg[1], w->segsums[0], w->segsums[1]};
+        for (void *p : old)
+            if (p) cudaFree(p);
+        w->ckpt = w->seg[0] = w->seg[1] = w->segsums[0] = w->segsums[1] = nullptr;
+        // a second segment buffer only when there is a segment to recompute while another is reversed
+        const int nbuf = nck > 1 ? 2 : 1;
+        bool ok = cudaMalloc(&w->ckpt, (size_t)nck * 6 * ld * 8) == cudaSuccess;
+        for (int q = 0; q < nbuf && ok; ++q)
+            ok = cudaMalloc(&w->seg[q], (size_t)K * 3 * 6 * ld * 8) == cudaSuccess &&
+                 cudaMalloc(&w->segsums[q], (size_t)K * 3 * 9 * np * 8) == cudaSuccess;
+        if (!ok) {
             cudaGetLastError();
             return set_err(PN_ERR_NOMEM, "checkpoints");
         }
@@ -1123,15 +1176,15 @@ extern "C" int pn_adj_forward(pn_ctx *c, int nsteps, int checkpoint_every) {
         w->nck = nck;
     }
     w->time0 = c->time;
-    w->seg_holds = -1;
+    w->holds[0] = w->holds[1] = -1;
     for (int k = 0; k < nck; ++k) {
         CU(cudaMemcpyAsync(w->ckpt + (size_t)k * 6 * ld, c->st.x, 6 * ld * 8, cudaMemcpyDeviceToDevice, c->stream));
         const int steps = (k + 1) * K <= nsteps ? K : nsteps - k * K;
         // the last segment keeps its stages now, so the backward pass need not recompute it
-        rc = k == nck - 1 ? record_segment(c, steps) : pn_steps(c, steps);
+        rc = k == nck - 1 ? record_segment(c, steps, k & 1, c->stream) : pn_steps(c, steps);
         if (rc) return rc;
     }
-    w->seg_holds = nck - 1;
+    w->holds[(nck - 1) & 1] = nck - 1;
     return check_device_err(c);
 }
 
@@ -1162,22 +1215,46 @@ extern "C" int pn_adj_backward(pn_ctx *c, const double *xbar_T, const double *vb
     sa.Xb = Xb; sa.Vb = Vb; sa.xb = xb; sa.vb = vb; sa.x1b = x1b; sa.v1b = v1b; sa.x2b = x2b; sa.v2b = v2b;
     sa.ab = ab; sa.xF = xF; sa.vF = vF; sa.h = h; sa.n = c->n; sa.ld = LD;
     const double time_final = c->time;
-    for (int k = w->nck - 1; k >= 0; --k) {
-        const int steps = (k + 1) * w->K <= w->nsteps ? w->K : w->nsteps - k * w->K;
-        // recompute the segment from its checkpoint, keeping every stage's evaluation state and
-        // pair sums (the last segment's are kept by the forward pass)
-        if (w->seg_holds != k) {
-            CU(cudaMemcpyAsync(c->st.x, w->ckpt + (size_t)k * 6 * ld, 6 * ld * 8, cudaMemcpyDeviceToDevice, s));
-            int rc = record_segment(c, steps);
+    // Two streams: the context's (s) reverses segment k while w->s2 recomputes segment k - 1 from
+    // its checkpoint into the other segment buffer (the recomputation uses the context's state and
+    // evaluation buffers, the reversal the VJP's own), so the O(N) kernels of each fill the
+    // other's gaps.  ev_rec[b]: buffer b holds its segment; ev_done[b]: its reversal is done.
+    cudaStream_t s2 = w->s2;
+    auto segsteps = [&](int k) { return (k + 1) * w->K <= w->nsteps ? w->K : w->nsteps - k * w->K; };
+    bool done_valid[2] = {false, false};
+    auto recompute = [&](int k) -> int {
+        const int b = k & 1;
+        if (done_valid[b]) CU(cudaStreamWaitEvent(s2, w->ev_done[b], 0));
+        CU(cudaMemcpyAsync(c->st.x, w->ckpt + (size_t)k * 6 * ld, 6 * ld * 8, cudaMemcpyDeviceToDevice, s2));
+        int rc = record_segment(c, segsteps(k), b, s2);
+        if (rc) return rc;
+        CU(cudaEventRecord(w->ev_rec[b], s2));
+        w->holds[b] = k;
+        return PN_OK;
+    };
+    CU(cudaEventRecord(w->ev_sync, s));  // everything queued so far (the forward pass, Xb) first
+    CU(cudaStreamWaitEvent(s2, w->ev_sync, 0));
+    const int klast = w->nck - 1;
+    if (w->holds[klast & 1] == klast) {
+        CU(cudaEventRecord(w->ev_rec[klast & 1], s));  // recorded by the forward pass on s
+    } else {
+        int rc = recompute(klast);
+        if (rc) return rc;
+    }
+    for (int k = klast; k >= 0; --k) {
+        const int b = k & 1;
+        if (k >= 1) {  // queue the next segment's recomputation first, so that it overlaps
+            int rc = recompute(k - 1);
             if (rc) return rc;
-            w->seg_holds = k;
         }
+        CU(cudaStreamWaitEvent(s, w->ev_rec[b], 0));
+        const int steps = segsteps(k);
         // reverse the segment's steps
         for (int t = steps - 1; t >= 0; --t) {
-            const double *S0 = w->seg + ((size_t)t * 3 + 0) * 6 * ld;
-            const double *S1 = w->seg + ((size_t)t * 3 + 1) * 6 * ld;
-            const double *S2 = w->seg + ((size_t)t * 3 + 2) * 6 * ld;
-            const double *ss = w->segsums + (size_t)t * 3 * 9 * np;
+            const double *S0 = w->seg[b] + ((size_t)t * 3 + 0) * 6 * ld;
+            const double *S1 = w->seg[b] + ((size_t)t * 3 + 1) * 6 * ld;
+            const double *S2 = w->seg[b] + ((size_t)t * 3 + 2) * 6 * ld;
+            const double *ss = w->segsums[b] + (size_t)t * 3 * 9 * np;
             // stage 3 evaluated a2 = F(x2, v2); stage 2 a1 = F(x1, v1); stage 1 a0 = F(x, v)
             sa.which = 0;
             k_stage_adj<<<nblk, nthreads, 0, s>>>(sa);
@@ -1195,7 +1272,11 @@ extern "C" int pn_adj_backward(pn_ctx *c, const double *xbar_T, const double *vb
             k_stage_adj<<<nblk, nthreads, 0, s>>>(sa);
             CU(cudaGetLastError());
         }
+        CU(cudaEventRecord(w->ev_done[b], s));
+        done_valid[b] = true;
     }
+    CU(cudaEventRecord(w->ev_sync, s2));  // the context's state is restored after the last recompute
+    CU(cudaStreamWaitEvent(s, w->ev_sync, 0));
     CU(cudaMemcpyAsync(hb.data(), Xb, 6 * ld * 8, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(m0bar, w->m0bar + 1, 8, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(c->st.x, final_state.data(), 6 * ld * 8, cudaMemcpyHostToDevice, s));
