@@ -135,7 +135,7 @@ static PairCfg choose_cfg(const pn_ctx *c, int mode, int nstar) {
     // j-splits for about 8 waves of 4 CTAs per SM, keeping >= 4 tiles per split
     int g = c->p.grid_split > 0 ? c->p.grid_split : (8 * c->sms * 4 + nib - 1) / (nib > 0 ? nib : 1);
     if (c->p.grid_split <= 0) {
-        if (g > 32) g = 32;
+        if (g > (nstar >= 65536 ? 8 : 32)) g = nstar >= 65536 ? 8 : 32;
         if (g > ntiles / 4) g = ntiles / 4;
     }
     if (g > ntiles) g = ntiles;

@@ -114,6 +114,9 @@ std::vector<PairCfg> tune_candidates(bool f32, int mode, int nstar, int sms) {
             const int ntiles = (nstar + c.tj - 1) / c.tj;
             for (int g : gs) {
                 if (g > 1 && g > ntiles / 4) break;  // keep >= 4 tiles per j-range
+                // large systems: at most 8 j-range splits; more saved < 0.3 % of the sweep (ncu
+                // launch list at N = 2^18) and cost 72 B per star and split of partial sums
+                if (big && g > 8) break;
                 c.gsplit = g;
                 c.x2 = 0;
                 // large mixed-precision systems: the packed sweep only (the scalar one measured
