@@ -837,7 +837,8 @@ struct AdjointWork {
     void *vpack = nullptr;
     TileOrigin *vtorg = nullptr;
     double *vspos = nullptr, *vpart = nullptr, *vglob = nullptr;
-    cudaStream_t s2 = nullptr;     // recomputation stream
+    cudaStream_t s2 = nullptr;     // recomputation stream (default priority)
+    cudaStream_t s1 = nullptr;     // reversal stream (highest priority: the critical path)
     cudaEvent_t ev_rec[2] = {}, ev_done[2] = {}, ev_sync = nullptr;
     double time0 = 0.0;
 };
@@ -848,6 +849,7 @@ void free_adjoint(pn_ctx *c) {
     AdjointWork *w = c->adj;
     if (!w) return;
     if (w->s2) cudaStreamSynchronize(w->s2);
+    if (w->s1) cudaStreamSynchronize(w->s1);
     void *b[] = {w->sums, w->apack, w->sdir, w->vdir, w->vjp, w->gbar, w->part, w->m0bar, w->tickets,
                  w->work, w->ckpt, w->seg[0], w->seg[1], w->segsums[0], w->segsums[1], w->sympart, w->symsum,
                  w->vpack, w->vtorg, w->vspos, w->vpart, w->vglob};
@@ -859,6 +861,7 @@ void free_adjoint(pn_ctx *c) {
     }
     if (w->ev_sync) cudaEventDestroy(w->ev_sync);
     if (w->s2) cudaStreamDestroy(w->s2);
+    if (w->s1) cudaStreamDestroy(w->s1);
     delete w;
     c->adj = nullptr;
 }
@@ -891,7 +894,10 @@ static int adj_ensure(pn_ctx *c) {
         free_adjoint(c);
         return set_err(PN_ERR_NOMEM, "adjoint buffers");
     }
-    bool ev_ok = cudaStreamCreateWithFlags(&w->s2, cudaStreamNonBlocking) == cudaSuccess &&
+    int prio_low = 0, prio_high = 0;
+    bool ev_ok = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high) == cudaSuccess &&
+                 cudaStreamCreateWithFlags(&w->s2, cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaStreamCreateWithPriority(&w->s1, cudaStreamNonBlocking, prio_high) == cudaSuccess &&
                  cudaEventCreateWithFlags(&w->ev_sync, cudaEventDisableTiming) == cudaSuccess;
     for (int q = 0; q < 2 && ev_ok; ++q)
         ev_ok = cudaEventCreateWithFlags(&w->ev_rec[q], cudaEventDisableTiming) == cudaSuccess &&
@@ -1220,6 +1226,8 @@ extern "C" int pn_adj_backward(pn_ctx *c, const double *xbar_T, const double *vb
     // evaluation buffers, the reversal the VJP's own), so the O(N) kernels of each fill the
     // other's gaps.  ev_rec[b]: buffer b holds its segment; ev_done[b]: its reversal is done.
     cudaStream_t s2 = w->s2;
+    cudaStream_t s0 = s;  // the context's stream: host copies before and after
+    s = w->s1;            // the reversal, at the highest stream priority
     auto segsteps = [&](int k) { return (k + 1) * w->K <= w->nsteps ? w->K : w->nsteps - k * w->K; };
     bool done_valid[2] = {false, false};
     auto recompute = [&](int k) -> int {
@@ -1232,8 +1240,9 @@ extern "C" int pn_adj_backward(pn_ctx *c, const double *xbar_T, const double *vb
         w->holds[b] = k;
         return PN_OK;
     };
-    CU(cudaEventRecord(w->ev_sync, s));  // everything queued so far (the forward pass, Xb) first
+    CU(cudaEventRecord(w->ev_sync, s0));  // everything queued so far (the forward pass, Xb) first
     CU(cudaStreamWaitEvent(s2, w->ev_sync, 0));
+    CU(cudaStreamWaitEvent(s, w->ev_sync, 0));
     const int klast = w->nck - 1;
     if (w->holds[klast & 1] == klast) {
         CU(cudaEventRecord(w->ev_rec[klast & 1], s));  // recorded by the forward pass on s
@@ -1276,7 +1285,10 @@ extern "C" int pn_adj_backward(pn_ctx *c, const double *xbar_T, const double *vb
         done_valid[b] = true;
     }
     CU(cudaEventRecord(w->ev_sync, s2));  // the context's state is restored after the last recompute
-    CU(cudaStreamWaitEvent(s, w->ev_sync, 0));
+    CU(cudaStreamWaitEvent(s0, w->ev_sync, 0));
+    CU(cudaEventRecord(w->ev_rec[0], s));  // and after the last reversal
+    CU(cudaStreamWaitEvent(s0, w->ev_rec[0], 0));
+    s = s0;
     CU(cudaMemcpyAsync(hb.data(), Xb, 6 * ld * 8, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(m0bar, w->m0bar + 1, 8, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(c->st.x, final_state.data(), 6 * ld * 8, cudaMemcpyHostToDevice, s));
