@@ -40,7 +40,7 @@ enum GbarSlot : int { GB_A1 = 0, GB_B3X, GB_B3Y, GB_B3Z, GB_C, GB_PX, GB_PY, GB_
 
 // Threads per block of the O(N) adjoint kernels: their per-star FP64 work is heavy, so small
 // blocks spread a system of a few thousand stars over every SM.
-constexpr int VJP_ON_NT = 32;
+constexpr int VJP_ON_NT = 64;
 
 // ------------------------------------------------------------------ per-star adjoint
 struct FinVjpArgs {
@@ -637,9 +637,11 @@ __global__ void __launch_bounds__(sym_threads<T>(), (sym_min_blocks<T>()))
     }
 }
 
-// Per (star, sum): the star's slots over every tile, added in tile order in FP64.  Each thread
-// takes 16 bytes of consecutive stars (4 in FP32, 2 in FP64) with one vector load per tile, so
-// that enough bytes are in flight to stream the partial sums at HBM/L2 rate.
+// Per (star, sum): the star's slots over every tile, added in tile order.  Each thread takes 16
+// bytes of consecutive stars (4 in FP32, 2 in FP64) with one vector load per tile.  FP32 slots
+// are added with Kahan compensation in FP32 (the ordered sweep's numerics): converting each to
+// FP64 and adding there would put ~2 x tiles x N operations on GB300's 1/64-rate FP64 pipe, which
+// measured 148 us per VJP at N = 16,384 against ~20 us for the compensated FP32 sum.
 template <typename T> struct SymVec;
 template <> struct SymVec<float> { using V = float4; static constexpr int W = 4; };
 template <> struct SymVec<double> { using V = double2; static constexpr int W = 2; };
@@ -654,15 +656,25 @@ __global__ void __launch_bounds__(256) k_vjp_sym_reduce(const T *part, double *Y
     const V *src = reinterpret_cast<const V *>(part + (size_t)c * npad + i);
     const size_t stride = (size_t)NY * npad / W;  // one tile, in vectors
     double t[W];
-#pragma unroll
-    for (int e = 0; e < W; ++e) t[e] = 0.0;
+    if constexpr (W == 4) {
+        float sum[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 8
-    for (int b = 0; b < nt; ++b) {
-        const V x = src[(size_t)b * stride];
-        if constexpr (W == 4) {
-            t[0] += (double)x.x; t[1] += (double)x.y; t[2] += (double)x.z; t[3] += (double)x.w;
-        } else {
-            t[0] += (double)x.x; t[1] += (double)x.y;
+        for (int b = 0; b < nt; ++b) {
+            const V x = src[(size_t)b * stride];
+            kahan_add(sum[0], cmp[0], x.x);
+            kahan_add(sum[1], cmp[1], x.y);
+            kahan_add(sum[2], cmp[2], x.z);
+            kahan_add(sum[3], cmp[3], x.w);
+        }
+#pragma unroll
+        for (int e = 0; e < 4; ++e) t[e] = (double)sum[e] - (double)cmp[e];
+    } else {
+        t[0] = t[1] = 0.0;
+#pragma unroll 8
+        for (int b = 0; b < nt; ++b) {
+            const V x = src[(size_t)b * stride];
+            t[0] += (double)x.x;
+            t[1] += (double)x.y;
         }
     }
 #pragma unroll
