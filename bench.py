@@ -506,7 +506,7 @@ def long_run(nstars, precisions, nsteps, every, allowance, label):
 def profile_case(nstars, shape=None):
     """One mixed-precision force evaluation of the bench workload at nstars (ncu target);
     shape = "ipt,tile_j,grid_split[,pair_variant]" pins the packed sweep's launch shape (e.g. the
-    tuned one; pair_variant 3 = the build for 3 CTAs per SM)."""
+    tuned one; pair_variant 3 / 4 = the build for 3 / 4 CTAs per SM)."""
     import pn_gb300 as pn
     sysm = pn.config_plummer(nstars, SEED, BH_FRACTION)
     kw = {}
@@ -589,7 +589,8 @@ def headline(args, rank, world, dist):
         pairs = float(ns) * float(ns)
         achieved = pairs * flops_pair / (pair_launch_ms * 1e-3) / 1e12
         kname = {2: "k_pair2<MODE_FORCE> (packed f32x2)",
-                 3: "k_pair2<MODE_FORCE> (packed f32x2, 3 CTAs per SM)"}.get(st.pair_variant, "k_pair<float, MODE_FORCE>")
+                 3: "k_pair2<MODE_FORCE> (packed f32x2, 3 CTAs per SM)",
+                 4: "k_pair2<MODE_FORCE> (packed f32x2, 4 CTAs per SM)"}.get(st.pair_variant, "k_pair<float, MODE_FORCE>")
         line["roofline"] = {"bound": "fp32", "kernel": kname,
                             "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                             "frac": achieved / peak32, "traffic": None,
@@ -598,7 +599,7 @@ def headline(args, rank, world, dist):
                             "peak_source": "measured FP32 FMA throughput of this GPU (pn_probe_fma_peak)",
                             "pair_interactions_per_s": pairs / (pair_launch_ms * 1e-3)}
         prof = os.path.join(ROOT, "profiles", "pair_sweep_traffic.json")
-        if os.path.exists(prof) and ns == NSTARS and st.pair_variant in (2, 3):
+        if os.path.exists(prof) and ns == NSTARS and st.pair_variant in (2, 3, 4):
             try:  # DRAM bytes of one launch at this size and shape, from an ncu capture
                 pt = json.load(open(prof))
                 line["roofline"]["traffic"] = pt.get("k_pair2_force_f32_N262144_bytes_per_launch")
@@ -616,7 +617,7 @@ def headline(args, rank, world, dist):
         # k_prep reads x, v, m (56 B) and writes spos, the paired pack, the i-side pack (96 B; the
         # scalar pack's 64 B too when the scalar sweep runs); k_finish reads v, m, spos (56 B) and
         # the j-range partial sums (9 doubles per split), and reads/writes the stage state (168 B)
-        moved = 56 + (96 if st.pair_variant in (2, 3) else 160) + 56 + 72 * gs + 168
+        moved = 56 + (96 if st.pair_variant in (2, 3, 4) else 160) + 56 + 72 * gs + 168
         algo = 104 + 144                  # BH-star O(N) terms + one stage update, per star
         peak_hbm = _measured_hbm_gbs()
         line["o_n_kernels"] = {"ms_per_evaluation": on_ms, "bytes_per_star_moved": moved,

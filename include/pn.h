@@ -67,12 +67,12 @@ typedef struct {
     int pair_variant;  /* mixed mode: PN_PAIR_AUTO (0, tuned), PN_PAIR_SCALAR (1),
                           PN_PAIR_F32X2 (2: packed FP32x2 instructions, two j per instruction) or
                           PN_PAIR_F32X2_OCC3 (3: the same with 2 i per thread, compiled for 3
-                          CTAs per SM) */
+                          CTAs per SM) or PN_PAIR_F32X2_OCC4 (4: ... for 4 CTAs per SM) */
     int integrator;    /* PN_INT_REFERENCE (0): the reference's 3-evaluation scheme
                           (Limit-sticky9.c:844-893); PN_INT_RK4 (1): classic 4th-order RK */
 } pn_params;
 
-enum { PN_PAIR_AUTO = 0, PN_PAIR_SCALAR = 1, PN_PAIR_F32X2 = 2, PN_PAIR_F32X2_OCC3 = 3 };
+enum { PN_PAIR_AUTO = 0, PN_PAIR_SCALAR = 1, PN_PAIR_F32X2 = 2, PN_PAIR_F32X2_OCC3 = 3, PN_PAIR_F32X2_OCC4 = 4 };
 enum { PN_INT_REFERENCE = 0, PN_INT_RK4 = 1 };
 
 /* Energies as the reference prints them (Limit-sticky9.c:561-562, :702-703). */
@@ -89,7 +89,7 @@ typedef struct {
     double total_ms;         /* whole force evaluation */
     double interactions;     /* star-star pairs evaluated by that launch */
     int tile_j, i_per_thread, j_split, grid_split, threads; /* launch shape used */
-    int pair_variant;        /* PN_PAIR_SCALAR, PN_PAIR_F32X2 or PN_PAIR_F32X2_OCC3: the kernel used */
+    int pair_variant;        /* PN_PAIR_SCALAR, PN_PAIR_F32X2, _OCC3 or _OCC4: the kernel used */
 } pn_stats;
 
 /* ------------------------------------------------------------------ 1. drop-in entry points */

@@ -28,7 +28,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libpn.so")
 PN_OK = 0
 PN_PREC_FP64 = 0
 PN_PREC_MIXED = 1
-PN_PAIR_AUTO, PN_PAIR_SCALAR, PN_PAIR_F32X2, PN_PAIR_F32X2_OCC3 = 0, 1, 2, 3
+PN_PAIR_AUTO, PN_PAIR_SCALAR, PN_PAIR_F32X2, PN_PAIR_F32X2_OCC3, PN_PAIR_F32X2_OCC4 = 0, 1, 2, 3, 4
 PN_NMAX = 270000
 
 _STATUS = {0: "PN_OK", -1: "PN_ERR_INVALID", -2: "PN_ERR_CUDA", -3: "PN_ERR_NOMEM",

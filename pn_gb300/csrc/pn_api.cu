@@ -115,10 +115,11 @@ static PairCfg choose_cfg(const pn_ctx *c, int mode, int nstar) {
         if (tuned.gsplit > ntiles_t) tuned.gsplit = ntiles_t;
         return tuned;
     }
-    if ((pv == PN_PAIR_F32X2 || pv == PN_PAIR_F32X2_OCC3) && f32) {
+    if ((pv == PN_PAIR_F32X2 || pv == PN_PAIR_F32X2_OCC3 || pv == PN_PAIR_F32X2_OCC4) && f32) {
         if (k.ipt > 2) k.ipt = 2;
         if (k.js != 1) k.js = 1;
-        k.x2 = (pv == PN_PAIR_F32X2_OCC3 && k.ipt == 2 && mode_has_force(mode)) ? 2 : 1;
+        const bool occ = k.ipt == 2 && mode_has_force(mode);
+        k.x2 = (occ && pv == PN_PAIR_F32X2_OCC3) ? 2 : (occ && pv == PN_PAIR_F32X2_OCC4) ? 3 : 1;
     } else if (pv == PN_PAIR_AUTO && f32 && !explicit_shape) {
         // untuned default of the mixed sweep: the packed f32x2 form, 2 i per thread for
         // N >= 4096 (fastest in the tuner's measurements at N = 2^18: 111 ms vs 125 ms)
@@ -198,7 +199,7 @@ static int validate_params(const pn_params *p) {
         return PN_ERR_INVALID;
     if (p->i_per_thread < 0 || p->j_split < 0 || p->grid_split < 0 || p->grid_split > 64)
         return PN_ERR_INVALID;
-    if (p->pair_variant < PN_PAIR_AUTO || p->pair_variant > PN_PAIR_F32X2_OCC3) return PN_ERR_INVALID;
+    if (p->pair_variant < PN_PAIR_AUTO || p->pair_variant > PN_PAIR_F32X2_OCC4) return PN_ERR_INVALID;
     if (p->integrator != PN_INT_REFERENCE && p->integrator != PN_INT_RK4) return PN_ERR_INVALID;
     if ((p->i_per_thread || p->j_split) &&
         !pair_shape_supported(p->i_per_thread ? p->i_per_thread : 1, p->j_split ? p->j_split : 1))
@@ -363,7 +364,10 @@ int pn::eval_force(pn_ctx *c, const double *x, const double *v, const double *m,
     if (timed) CU(cudaEventRecord(c->ev2, s));
     c->stats.tile_j = k.tj; c->stats.i_per_thread = k.ipt; c->stats.j_split = k.js;
     c->stats.grid_split = k.gsplit; c->stats.threads = PAIR_NT;
-    c->stats.pair_variant = k.x2 == 2 ? PN_PAIR_F32X2_OCC3 : k.x2 ? PN_PAIR_F32X2 : PN_PAIR_SCALAR;
+    c->stats.pair_variant = k.x2 == 3   ? PN_PAIR_F32X2_OCC4
+                            : k.x2 == 2 ? PN_PAIR_F32X2_OCC3
+                            : k.x2      ? PN_PAIR_F32X2
+                                        : PN_PAIR_SCALAR;
     c->stats.interactions = (double)nstar * (double)nstar;
     return PN_OK;
 }
@@ -917,7 +921,7 @@ extern "C" int pn_bench_steps(pn_ctx *c, int nsteps, int flush_l2, double *step_
 // rsqrt as 1 and every other add/multiply as 1 (the operations written in pn_device.cuh).
 extern "C" double pn_flops_per_pair(int mode, int precision, int pair_variant) {
     const bool f32 = precision == PN_PREC_MIXED;
-    if (f32 && (pair_variant == PN_PAIR_F32X2 || pair_variant == PN_PAIR_F32X2_OCC3)) {
+    if (f32 && pair_variant >= PN_PAIR_F32X2 && pair_variant <= PN_PAIR_F32X2_OCC4) {
         // the packed sweep (operands pre-scaled): FORCE 50 FP32 operations of which 24 FMA,
         // NEWTON 22 (7 FMA), ENERGY 32 (12 FMA); FMA = 2 flops, the MUFU rsqrt = 1
         switch (mode) {

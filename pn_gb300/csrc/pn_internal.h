@@ -13,7 +13,7 @@ struct PairCfg {
     int tj = 128;    // stars per j-tile
     int gsplit = 1;  // j-range splits across CTAs
     int x2 = 0;      // FP32 only: the packed f32x2 sweep (pn_pair2.cuh; js = 1, ipt 1 or 2);
-                     // 2 = the same sized for 3 CTAs per SM (ipt 2, force sweeps)
+                     // 2 / 3 = the same sized for 3 / 4 CTAs per SM (ipt 2, force sweeps)
 };
 
 // Launches k_pair for the given precision/mode/shape (returns cudaErrorInvalidValue for an

@@ -28,8 +28,10 @@ static cudaError_t launch_two_mode(const PairCfg &c, const PairArgs &a, cudaStre
     if (c.js != 1 || !a.pack2 || !a.ipack) return cudaErrorInvalidValue;
     if (c.ipt == 1) return launch_two<MODE, 1, 4>(c, a, s);
     if (c.ipt == 2) {
-        if constexpr (mode_has_force(MODE))  // 3 CTAs per SM (x2 = 2): the force sweeps only
+        if constexpr (mode_has_force(MODE)) {  // 3 or 4 CTAs per SM (x2 = 2, 3): the force sweeps only
             if (c.x2 == 2) return launch_two<MODE, 2, 3>(c, a, s);
+            if (c.x2 == 3) return launch_two<MODE, 2, 4>(c, a, s);
+        }
         return launch_two<MODE, 2, 2>(c, a, s);
     }
     return cudaErrorInvalidValue;

@@ -47,7 +47,7 @@ void load_file_locked() {
         if (pair_shape_supported(e.cfg.ipt, e.cfg.js) && e.cfg.gsplit >= 1 && e.cfg.gsplit <= 64 &&
             (e.cfg.tj == 32 || e.cfg.tj == 64 || e.cfg.tj == 128 || e.cfg.tj == 256) &&
             (e.cfg.x2 == 0 || (e.cfg.x2 == 1 && e.cfg.js == 1 && e.cfg.ipt <= 2 && e.prec == 1) ||
-             (e.cfg.x2 == 2 && e.cfg.js == 1 && e.cfg.ipt == 2 && e.prec == 1)))
+             ((e.cfg.x2 == 2 || e.cfg.x2 == 3) && e.cfg.js == 1 && e.cfg.ipt == 2 && e.prec == 1)))
             g_table.push_back(e);
     }
     fclose(f);
@@ -125,8 +125,10 @@ std::vector<PairCfg> tune_candidates(bool f32, int mode, int nstar, int sms) {
                 if (f32 && js == 1 && ipt <= 2) {  // the packed f32x2 sweep of the same shape
                     c.x2 = 1;
                     out.push_back(c);
-                    if (ipt == 2 && mode != MODE_ENERGY) {  // ... sized for 3 CTAs per SM
+                    if (ipt == 2 && mode != MODE_ENERGY) {  // ... sized for 3 and 4 CTAs per SM
                         c.x2 = 2;
+                        out.push_back(c);
+                        c.x2 = 3;
                         out.push_back(c);
                     }
                 }

@@ -120,7 +120,9 @@ SHAPES = [dict(), dict(i_per_thread=1), dict(i_per_thread=4), dict(j_split=2), d
           dict(grid_split=7, tile_j=32, j_split=4),
           # the packed f32x2 sweep (mixed precision only; FP64 ignores the variant)
           dict(pair_variant=2), dict(pair_variant=2, i_per_thread=1, tile_j=32),
-          dict(pair_variant=2, i_per_thread=2, tile_j=256, grid_split=5)]
+          dict(pair_variant=2, i_per_thread=2, tile_j=256, grid_split=5),
+          dict(pair_variant=3, i_per_thread=2, tile_j=128, grid_split=3),
+          dict(pair_variant=4, i_per_thread=2, tile_j=256, grid_split=2)]
 
 
 @pytest.mark.parametrize("n", [1, 2, 3, 33, 64, 65, 129, 257, 1000])
