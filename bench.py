@@ -598,6 +598,12 @@ def headline(args, rank, world, dist):
                             "pair_launch_ms": pair_launch_ms,
                             "peak_source": "measured FP32 FMA throughput of this GPU (pn_probe_fma_peak)",
                             "pair_interactions_per_s": pairs / (pair_launch_ms * 1e-3)}
+        if st.pair_variant in (2, 3, 4):
+            # the same FMA work issued as packed two-lane instructions, as the packed sweep does:
+            # the ceiling of a sweep made only of fma.rn.f32x2
+            peak2 = pn.probe_fma_peak(pn.PROBE_F32X2)
+            line["roofline"]["peak_f32x2"] = peak2
+            line["roofline"]["frac_of_f32x2_peak"] = achieved / peak2
         prof = os.path.join(ROOT, "profiles", "pair_sweep_traffic.json")
         if os.path.exists(prof) and ns == NSTARS and st.pair_variant in (2, 3, 4):
             try:  # DRAM bytes of one launch at this size and shape, from an ncu capture

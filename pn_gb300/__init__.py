@@ -28,6 +28,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libpn.so")
 PN_OK = 0
 PN_PREC_FP64 = 0
 PN_PREC_MIXED = 1
+PROBE_F32X2 = 2  # pn_probe_fma_peak: FP32 as packed two-lane fma.rn.f32x2
 PN_PAIR_AUTO, PN_PAIR_SCALAR, PN_PAIR_F32X2, PN_PAIR_F32X2_OCC3, PN_PAIR_F32X2_OCC4 = 0, 1, 2, 3, 4
 PN_NMAX = 270000
 
@@ -537,7 +538,8 @@ def flops_per_pair(mode: int, precision: int, pair_variant: int = PN_PAIR_SCALAR
 
 
 def probe_fma_peak(precision: int) -> float:
-    """Measured FMA peak of this GPU in TFLOP/s (FP32 for PN_PREC_MIXED, FP64 otherwise)."""
+    """Measured FMA peak of this GPU in TFLOP/s: FP32 for PN_PREC_MIXED, FP64 for PN_PREC_FP64,
+    and FP32 issued as packed two-lane fma.rn.f32x2 instructions for 2 (PROBE_F32X2)."""
     t = np.zeros(1)
     _check(lib().pn_probe_fma_peak(int(precision), _p(t)), "pn_probe_fma_peak")
     return float(t[0])

@@ -947,6 +947,38 @@ template <typename T> __device__ __forceinline__ T probe_fma(T x, T a, T b);
 template <> __device__ __forceinline__ float probe_fma<float>(float x, float a, float b) { return fmaf(x, a, b); }
 template <> __device__ __forceinline__ double probe_fma<double>(double x, double a, double b) { return fma(x, a, b); }
 
+// packed FP32x2: both lanes of a 64-bit register pair in one fma.rn.f32x2
+struct F2 { unsigned long long v; };
+template <> __device__ __forceinline__ F2 probe_fma<F2>(F2 x, F2 a, F2 b) {
+    F2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(x.v), "l"(a.v), "l"(b.v));
+    return r;
+}
+static __device__ __forceinline__ F2 f2_of(float lo, float hi) {
+    F2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
+    return r;
+}
+static __global__ void k_fma2_probe(float *out, int iters, float a, float b) {
+    F2 r[8];
+    const F2 a2 = f2_of(a, a), b2 = f2_of(b, b);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) r[q] = f2_of((float)(threadIdx.x + q), (float)(threadIdx.x - q));
+    for (int it = 0; it < iters; it += 16)
+#pragma unroll
+        for (int u = 0; u < 16; ++u)
+#pragma unroll
+            for (int q = 0; q < 8; ++q) r[q] = probe_fma<F2>(r[q], a2, b2);
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        float lo, hi;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r[q].v));
+        s += lo + hi;
+    }
+    if (s == 123456.0f) out[threadIdx.x] = s;  // keeps the chains live
+}
+
 template <typename T>
 static __global__ void k_fma_probe(T *out, int iters, T a, T b) {
     T r[8];
@@ -965,6 +997,7 @@ static __global__ void k_fma_probe(T *out, int iters, T a, T b) {
 
 extern "C" int pn_probe_fma_peak(int precision, double *tflops) {
     if (!tflops) return set_err(PN_ERR_INVALID, "probe");
+    if (precision < PN_PREC_FP64 || precision > 2) return set_err(PN_ERR_INVALID, "probe: precision");
     if (pn_device_count() < 1) return set_err(PN_ERR_UNSUPPORTED, "no CUDA device");
     int dev = 0, sms = 0;
     CU(cudaGetDevice(&dev));
@@ -975,12 +1008,14 @@ extern "C" int pn_probe_fma_peak(int precision, double *tflops) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     const int threads = 256, blocks = sms * 8;
-    const int iters = precision == PN_PREC_MIXED ? 20000 : 1000;
+    const int iters = precision == PN_PREC_FP64 ? 1000 : 20000;
     float best = 1e30f;
     for (int rep = 0; rep < 4; ++rep) {
         cudaEventRecord(e0);
         if (precision == PN_PREC_MIXED)
             k_fma_probe<float><<<blocks, threads>>>((float *)out, iters, 0.9999f, 1e-4f);
+        else if (precision == 2)
+            k_fma2_probe<<<blocks, threads>>>((float *)out, iters / 2, 0.9999f, 1e-4f);
         else
             k_fma_probe<double><<<blocks, threads>>>((double *)out, iters, 0.9999, 1e-4);
         cudaEventRecord(e1);
@@ -994,6 +1029,7 @@ extern "C" int pn_probe_fma_peak(int precision, double *tflops) {
     cudaEventDestroy(e1);
     cudaFree(out);
     if (e != cudaSuccess) return set_err(PN_ERR_CUDA, "probe: %s", cudaGetErrorString(e));
+    // the packed probe runs iters / 2 instructions of two lanes each: the same flops
     const double flops = 2.0 * 8.0 * (double)iters * threads * (double)blocks;
     *tflops = flops / (best * 1e-3) / 1e12;
     return PN_OK;

@@ -254,6 +254,18 @@ def test_bounded_wait_times_out_cleanly(pn):
         assert np.isfinite(c.force()).all()
 
 
+def test_fma_peak_probes(pn):
+    """The roofline denominators: FP32 FMA, the same issued as packed fma.rn.f32x2, and FP64
+    (GB300's FP64 rate is a small fraction of FP32's); an unknown probe is rejected."""
+    f32 = pn.probe_fma_peak(pn.PN_PREC_MIXED)
+    f2 = pn.probe_fma_peak(pn.PROBE_F32X2)
+    f64 = pn.probe_fma_peak(pn.PN_PREC_FP64)
+    assert f32 > 0 and f2 > 0 and 0 < f64 < 0.25 * f32, (f32, f2, f64)
+    assert f2 <= 1.1 * f32, (f32, f2)  # two lanes per instruction, the same FMA units
+    t = np.zeros(1)
+    assert pn.lib().pn_probe_fma_peak(3, t.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == -1
+
+
 # ------------------------------------------------------------------ drop-in entry points
 def test_dropin_force_and_energy_output(pn, oracle, capfd):
     x, v, m = random_system(1001, 21)
