@@ -525,21 +525,37 @@ def profile_case(nstars, shape=None):
 
 
 def host_stage_step(pn, x, v, m, eps, dt):
-    """The reference main loop's step around the drop-in force() (Limit-sticky9.c:844-893)."""
+    """The reference main loop's step around the drop-in force() (Limit-sticky9.c:844-893), the
+    stage arithmetic done in place (the same roundings as the reference's loops: 0.5 dt is exact)."""
     a = pn.force(x, v, m, eps)
-    x1 = x + 0.5 * v * dt
-    v1 = v + 0.5 * a * dt
+    x1 = v * (0.5 * dt)
+    x1 += x
+    v1 = a * (0.5 * dt)
+    v1 += v
     h = x1.copy()
     hv = v1.copy()
     a = pn.force(x1, v1, m, eps)
-    x1 = x + 0.5 * v1 * dt
-    v1 = v + 0.5 * a * dt
+    np.multiply(v1, 0.5 * dt, out=x1)
+    x1 += x
+    np.multiply(a, 0.5 * dt, out=v1)
+    v1 += v
     h += x1
     hv += v1
     a = pn.force(x1, v1, m, eps)
-    x3 = x + v1 * dt
-    v3 = v + a * dt
-    return (x + x3 + 2.0 * h) / 6.0, (v + v3 + 2.0 * hv) / 6.0
+    # (x + x3 + 2 h) / 6 with x3 = x + v1 dt, and the same for v
+    np.multiply(v1, dt, out=x1)
+    x1 += x
+    x1 += x
+    h *= 2.0
+    x1 += h
+    x1 /= 6.0
+    np.multiply(a, dt, out=v1)
+    v1 += v
+    v1 += v
+    hv *= 2.0
+    v1 += hv
+    v1 /= 6.0
+    return x1, v1
 
 
 # ---------------------------------------------------------------------------- headline
