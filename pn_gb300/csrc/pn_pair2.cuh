@@ -58,7 +58,9 @@ __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
     return r;
 }
 __device__ __forceinline__ void lds2(const void *p, f2 &a, f2 &b) {
-    asm volatile("ld.shared.v2.b64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "r"(smem_u32(p)));
+    const ulonglong2 u = *static_cast<const ulonglong2 *>(p);
+    a = u.x;
+    b = u.y;
 }
 // K times the inverse square root of both lanes: MUFU rsqrt each, refined by one Newton-Raphson
 // step y' = y (1.5 - 0.5 x y^2) whose two constants are scaled by K (exact in FP32).
