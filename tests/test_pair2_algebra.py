@@ -1,4 +1,5 @@
-"""The packed FP32x2 pair sweep's arithmetic (pn_pair2.cuh) restated in numpy.
+"""The pair sweeps' arithmetic restated in numpy: the packed FP32x2 form (pn_pair2.cuh) and the
+scalar form of the FP32 and FP64 sweeps (pn_device.cuh).
 
 The packed sweep evaluates the pair sums of pn_device.cuh (G, Phi, S0, U, W and Psi) from
 scaled operands: positions as hi/lo pairs relative to a tile origin, m / K^3, mu3 / K, k35 / K,
@@ -8,7 +9,7 @@ w = sqrt(3) v, c1 - 2|v|^2 and c3 (k_prep's paired pack), the i side's 4/sqrt(3)
 Here the same operations, in the same order, run in float64 with K = 1/sqrt(2) and are checked
 against the sums written from their definitions (the algebra), and in float32 with the
 kernel's K and an emulated FMA (the rounding stays at a few units of FP32 rounding of the
-absolute term sums).  Everything runs on the CPU.
+absolute term sums).  The scalar form is checked the same way.  Everything runs on the CPU.
 """
 import numpy as np
 import pytest
@@ -128,19 +129,76 @@ def _packed(s, v, m, m0, eps, i, mode, dt, K=X2_K):
     return out
 
 
-@pytest.mark.parametrize("mode", ["force", "force_energy", "energy"])
-def test_packed_sums_equal_definitions_in_float64(mode):
+def _scalar(s, v, m, m0, eps, i, mode, dt, K=None):
+    """pair_accumulate (pn_device.cuh) over all j, the scalar form of the FP32 and FP64 sweeps:
+    unscaled pack (hi, lo, m | mu3 | v, qe | c1, c3, k35), the MUFU rsqrt refined as
+    y + (y/2)(1 - x y^2) in FP32 (FP64: rsqrt), cv dv accumulated per pair."""
+    A = _Arith(dt)
+    eps2 = eps * eps
+    R = ((s * s).sum(1) + eps2) ** -0.5
+    mu3 = m * R ** 3
+    c1, c3, k35 = 1.25 * m0 * R, 0.25 * m0 * R ** 3, 3.5 * m0 * mu3
+    o = s[0]
+    if dt == np.float32:
+        hj, lj = _split(s - o, dt)
+        ei, li = _split(s[i] - o, dt)
+        d = [(hj[:, k] - ei[k]) + (lj[:, k] - li[k]) for k in range(3)]
+    else:
+        d = [s[:, k] - s[i, k] for k in range(3)]
+    jm, jmu3, jc1, jc3, jk35 = A.c(m), A.c(mu3), A.c(c1), A.c(c3), A.c(k35)
+    jv = A.c(v)
+    vf = v[i].astype(np.float32).astype(np.float64) if dt == np.float32 else v[i]
+    vi = A.c(vf)
+    vi2 = A.c((vf * vf).sum())
+    qe = A.c((s[i] * s[i]).sum() + eps2)
+    e2 = A.c(eps2)
+    rhoe = A.fma(d[2], d[2], A.fma(d[1], d[1], A.fma(d[0], d[0], e2)))
+    if dt == np.float32:
+        y = A.rsqrt(rhoe)
+        h = rhoe * y
+        Q = A.fma(A.c(0.5) * y, A.fma(-h, y, A.c(1.0)), y)
+    else:
+        Q = rhoe ** -0.5
+    Q2 = Q * Q
+    mQ = jm * Q
+    vdj = A.fma(jv[:, 2], d[2], A.fma(jv[:, 1], d[1], jv[:, 0] * d[0]))
+    vdi = A.fma(vi[2], d[2], A.fma(vi[1], d[1], vi[0] * d[0]))
+    if mode == "energy":
+        vivj = A.fma(vi[2], jv[:, 2], A.fma(vi[1], jv[:, 1], vi[0] * jv[:, 0]))
+        psi = A.fma(mQ, A.fma(A.c(7.0), vivj, (vdi * vdj) * Q2), 0)
+        return {"Phi": mQ.astype(np.float64).sum(), "Psi": psi.astype(np.float64).sum()}
+    mQ3 = mQ * Q2
+    dv = [jv[:, k] - vi[k] for k in range(3)]
+    dv2 = A.fma(dv[2], dv[2], A.fma(dv[1], dv[1], dv[0] * dv[0]))
+    br = A.fma(rhoe - qe, jc3, jc1)
+    br = br + A.fma(A.c(-2.0), dv2, vi2)
+    br = A.fma(A.c(1.5), (vdj * vdj) * Q2, br)
+    cd = A.fma(mQ3, br, jk35 * Q)
+    cv = mQ3 * A.fma(A.c(4.0), vdi, A.c(-3.0) * vdj)
+    return {"G": np.array([(mQ3 * d[k]).astype(np.float64).sum() for k in range(3)]),
+            "Phi": mQ.astype(np.float64).sum(), "S0": mQ3.astype(np.float64).sum(),
+            "U": (jmu3 * Q).astype(np.float64).sum(),
+            "W": np.array([A.fma(cd, d[k], cv * dv[k]).astype(np.float64).sum() for k in range(3)])}
+
+
+FORMS = {"packed": _packed, "scalar": _scalar}
+
+
+@pytest.mark.parametrize("form,mode", [("packed", "force"), ("packed", "force_energy"), ("packed", "energy"),
+                                       ("scalar", "force"), ("scalar", "energy")])
+def test_sweep_sums_equal_definitions_in_float64(form, mode):
     s, v, m, m0, eps = _system(300, 1)
     for i in (0, 1, 5, 77, 299):  # the tile-origin star, halo stars, core stars
         ref, scale = _definitions(s, v, m, m0, eps, i)
-        got = _packed(s, v, m, m0, eps, i, mode, np.float64, K=np.sqrt(0.5))
+        got = FORMS[form](s, v, m, m0, eps, i, mode, np.float64, K=np.sqrt(0.5))
         for key, val in got.items():
             err = np.max(np.abs(np.asarray(val) - np.asarray(ref[key])))
             assert err <= 1e-12 * scale[key], (mode, i, key, err, scale[key])
 
 
+@pytest.mark.parametrize("form", ["packed", "scalar"])
 @pytest.mark.parametrize("mode", ["force", "energy"])
-def test_packed_sums_float32_rounding_level(mode):
+def test_sweep_sums_float32_rounding_level(form, mode):
     """In float32 every sum stays within a few units of FP32 rounding (u = 2^-24) of the sum of
     its terms' magnitudes; the velocity inputs are rounded to FP32 as the kernel's are."""
     s, v, m, m0, eps = _system(2048, 2)
@@ -148,7 +206,7 @@ def test_packed_sums_float32_rounding_level(mode):
     worst = {}
     for i in range(0, 2048, 97):
         ref, scale = _definitions(s, v.astype(np.float32).astype(np.float64), m, m0, eps, i)
-        got = _packed(s, v, m, m0, eps, i, mode, np.float32)
+        got = FORMS[form](s, v, m, m0, eps, i, mode, np.float32)
         for key, val in got.items():
             r = np.max(np.abs(np.asarray(val) - np.asarray(ref[key]))) / (u * scale[key])
             worst[key] = max(worst.get(key, 0.0), float(r))
