@@ -68,6 +68,11 @@ def test_invalid_arguments(pn):
     p = pn.default_params(tile_j=48)
     assert pn.lib().pn_create(ctypes.byref(h), 100, ctypes.byref(p)) == -1
     assert pn.lib().pn_create(ctypes.byref(h), 0, None) == -1
+    # the peak probes: FP64, FP32, packed FP32x2 (0..2); anything else or no output is invalid
+    t = np.zeros(1)
+    assert pn.lib().pn_probe_fma_peak(3, pn._p(t)) == -1
+    assert pn.lib().pn_probe_fma_peak(-1, pn._p(t)) == -1
+    assert pn.lib().pn_probe_fma_peak(pn.PN_PREC_MIXED, None) == -1
 
 
 def test_uniform_sphere_deterministic(pn):
