@@ -57,6 +57,10 @@ __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
     return r;
 }
+// One 128-bit shared-memory load of a pack group: two f32x2 operands.  A plain C++ load, so the
+// compiler can schedule it among the arithmetic (an asm volatile load issued 6 % more
+// instructions and ran 2 % slower); it cannot move above the tile's arrival, which the
+// mbarrier wait (an asm with a memory clobber) orders before it.
 __device__ __forceinline__ void lds2(const void *p, f2 &a, f2 &b) {
     const ulonglong2 u = *static_cast<const ulonglong2 *>(p);
     a = u.x;
