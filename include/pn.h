@@ -185,8 +185,9 @@ int pn_bench_steps(pn_ctx *ctx, int nsteps, int flush_l2, double *step_ms, doubl
  * form); an FMA counts 2, the MUFU rsqrt 1, any other add or multiply 1. */
 double pn_flops_per_pair(int mode, int precision, int pair_variant);
 /* Measured FMA throughput of this GPU (TFLOP/s, FMA = 2 flops) in FP32 (PN_PREC_MIXED), FP64
- * (PN_PREC_FP64) or, with precision 2, FP32 issued as the packed two-lane fma.rn.f32x2 that the
- * packed sweep uses: the roofline denominators of the pair sweeps. */
+ * (PN_PREC_FP64) or FP32 issued as the packed two-lane fma.rn.f32x2 that the packed sweep uses
+ * (PN_PROBE_F32X2): the roofline denominators of the pair sweeps. */
+enum { PN_PROBE_F32X2 = 2 };
 int pn_probe_fma_peak(int precision, double *tflops);
 
 /* Self-test of the in-kernel bounded waits: launches a kernel whose mbarrier wait can only end

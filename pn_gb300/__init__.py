@@ -28,7 +28,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libpn.so")
 PN_OK = 0
 PN_PREC_FP64 = 0
 PN_PREC_MIXED = 1
-PROBE_F32X2 = 2  # pn_probe_fma_peak: FP32 as packed two-lane fma.rn.f32x2
+PROBE_F32X2 = 2  # PN_PROBE_F32X2: pn_probe_fma_peak of FP32 as packed two-lane fma.rn.f32x2
 PN_PAIR_AUTO, PN_PAIR_SCALAR, PN_PAIR_F32X2, PN_PAIR_F32X2_OCC3, PN_PAIR_F32X2_OCC4 = 0, 1, 2, 3, 4
 PN_NMAX = 270000
 

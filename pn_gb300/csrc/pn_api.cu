@@ -997,7 +997,7 @@ static __global__ void k_fma_probe(T *out, int iters, T a, T b) {
 
 extern "C" int pn_probe_fma_peak(int precision, double *tflops) {
     if (!tflops) return set_err(PN_ERR_INVALID, "probe");
-    if (precision < PN_PREC_FP64 || precision > 2) return set_err(PN_ERR_INVALID, "probe: precision");
+    if (precision < PN_PREC_FP64 || precision > PN_PROBE_F32X2) return set_err(PN_ERR_INVALID, "probe: precision");
     if (pn_device_count() < 1) return set_err(PN_ERR_UNSUPPORTED, "no CUDA device");
     int dev = 0, sms = 0;
     CU(cudaGetDevice(&dev));
@@ -1014,7 +1014,7 @@ extern "C" int pn_probe_fma_peak(int precision, double *tflops) {
         cudaEventRecord(e0);
         if (precision == PN_PREC_MIXED)
             k_fma_probe<float><<<blocks, threads>>>((float *)out, iters, 0.9999f, 1e-4f);
-        else if (precision == 2)
+        else if (precision == PN_PROBE_F32X2)
             k_fma2_probe<<<blocks, threads>>>((float *)out, iters / 2, 0.9999f, 1e-4f);
         else
             k_fma_probe<double><<<blocks, threads>>>((double *)out, iters, 0.9999, 1e-4);
