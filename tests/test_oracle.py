@@ -82,6 +82,47 @@ def test_against_reference_live(oracle, n):
     assert np.array_equal(xa, xb) and np.array_equal(va, vb)
 
 
+def _edge_system(kind, n=40):
+    rng = np.random.default_rng(7)
+    x = rng.uniform(-1, 1, (n, 3))
+    v = rng.normal(0, 0.3, (n, 3))
+    m = rng.uniform(0.5, 1.5, n) / n
+    m[0] = 0.05
+    if kind == "moving_offset_bh":  # the BH away from the origin and moving
+        x[0] = [0.4, -0.7, 0.2]
+        v[0] = [0.05, 0.02, -0.03]
+    elif kind == "coincident_stars":  # star pairs at identical positions (softened, finite)
+        x[0] = [0.0, 0.0, 0.1]
+        x[5] = x[6] = x[7]
+        v[5] = -v[6]
+    elif kind == "wide_scales":  # a tight core and a far halo: 1e-4 .. 1e3
+        x[0] = 0.0
+        x[1:] *= np.exp(rng.uniform(np.log(1e-4), np.log(1e3), (n - 1, 1)))
+    elif kind == "mass_ratios":  # stars from 1e-9 to 1e-1 of a heavy BH
+        m[0] = 10.0
+        m[1:] = np.exp(rng.uniform(np.log(1e-9), np.log(1e-1), n - 1))
+    return x, v, m
+
+
+@pytest.mark.parametrize("kind", ["moving_offset_bh", "coincident_stars", "wide_scales", "mass_ratios"])
+def test_against_reference_live_edge_cases(oracle, kind):
+    """Bit-exact against the reference compiled from its source, on inputs the reference's own
+    loops treat as edge cases: the BH off the origin and moving (every BH-relative term and the
+    BH's own 1PN acceleration, Limit-sticky9.c:54-97), coincident stars, 7 decades of radius,
+    8 decades of mass."""
+    if not oracle.ref_available():
+        pytest.skip("reference source not present on this machine")
+    x, v, m = _edge_system(kind)
+    eps = 0.01
+    a = oracle.force(x, v, m, eps)
+    assert np.isfinite(a).all()
+    assert np.array_equal(a, oracle.ref_force(x, v, m, eps))
+    assert oracle.energy(x, v, m, eps)[3] == oracle.ref_initial_energy(x, v, m, eps)
+    xa, va = oracle.run(x, v, m, eps, 1e-4, 2)
+    xb, vb = oracle.ref_run(x, v, m, eps, 1e-4, 2)
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+
+
 def test_quirk_scheme_is_state_averaging(oracle):
     """Limit-sticky9.c:841-893: three force() calls and an average of the stage STATES, so a
     force-free particle advances by dt*(v+v+v)/6 = v*dt/2 per step (first order)."""
